@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark of the isosurface hot path.
+
+Workload (one step): plain MarchingCubes(iso=0f0) on a 1024^3 Float32 volume
+f = sum_{k=1..16} a_k sin(2pi w_k.p + phi_k) over [0,1]^3 (X = Y = Z = 0:1,
+seeded a_k ~ N(0,1), |w_k| ~ U[1,8] with a random direction, phi_k ~ U[0,2pi)).
+The volume is 4 GiB, larger than L2, so no flush is needed between steps.
+
+Metric: Gvoxels/s counting input samples nx*ny*nz.
+  value  -- device-resident: mesh_extract_device (classify -> scan -> emit)
+            with the volume and preallocated outputs in HBM;
+  e2e    -- the two-phase drop-in call (mesh_count + mesh_fill) with pinned
+            host buffers: upload, extraction and download of the mesh.
+The roofline object reports the dominant kernel's algorithmic bytes over its
+CUDA-event time; `pipeline` reports in+out bytes over the whole step.
+
+--impl reference times the reference algorithm on the host cores instead:
+the CPU restatement of Meshing.jl's MarchingCubes (single-threaded, as the
+reference is) on a z slab of the same field.
+Multi-GPU (torchrun): independent replicas, weak scaling.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 1024
+SEED = 0
+WORKLOAD = ('MarchingCubes(iso=0f0) on a %d^3 Float32 16-term random-sines field over [0,1]^3 '
+            '(X=Y=Z=0:1), Julia column-major layout')
+
+
+def sines_host(n, z0, nz, seed=SEED):
+    """numpy version of meshing_gb300.fields.sines for a z slab: C-ordered (nz, n, n) float32."""
+    import meshing_gb300.fields as fields  # noqa: F401  (parameters only)
+    g = np.linspace(0.0, 1.0, n)
+    out = np.zeros((nz, n, n), np.float32)
+    for a, w, ph in fields.sines_params(seed):
+        ex = np.exp(1j * (2 * np.pi * w[0]) * g).astype(np.complex64)
+        ey = np.exp(1j * (2 * np.pi * w[1]) * g).astype(np.complex64)
+        ez = np.exp(1j * ((2 * np.pi * w[2]) * g[z0:z0 + nz] + ph)).astype(np.complex64)
+        for k in range(nz):
+            out[k] += np.float32(a) * (ez[k] * (ey[:, None] * ex[None, :])).imag
+    return out
+
+
+def sines_device(n, seed=SEED, device='cuda'):
+    """The benchmark field on the device, Julia layout (x fastest), float32."""
+    import torch
+    import meshing_gb300.fields as fields
+    g = torch.linspace(0.0, 1.0, n, dtype=torch.float64, device=device)
+    out = torch.zeros((n, n, n), dtype=torch.float32, device=device)
+    zc = 64
+    for a, w, ph in fields.sines_params(seed):
+        ax = ((2 * math.pi * w[0]) * g).float()
+        ay = ((2 * math.pi * w[1]) * g).float()
+        az = ((2 * math.pi * w[2]) * g + ph).float()
+        for z0 in range(0, n, zc):
+            arg = az[z0:z0 + zc, None, None] + ay[None, :, None] + ax[None, None, :]
+            out[z0:z0 + zc].add_(torch.sin(arg), alpha=float(a))
+    return out.permute(2, 1, 0)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(index), '--query-gpu=' + self.Q, '--format=csv,noheader',
+                                       '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(',') for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            try:
+                sm.append(float(r[1].split()[0]))
+                mx = float(r[2].split()[0])
+                for nm, v in zip(names, r[5:9]):
+                    if 'Active' in v and 'Not' not in v:
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': mx, 'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peak():
+    try:
+        j = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+        return float(j['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+def cpu_baseline(n, planes, steps=1, warmup=0):
+    """Oracle (CPU restatement of MarchingCubes) on a z slab of the field: Gvoxels/s."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle
+    slab = sines_host(n, 0, planes + 1)          # C-ordered (nz, n, n) == Julia layout (n, n, nz)
+    A = slab.transpose(2, 1, 0)                  # Fortran view, shape (n, n, nz)
+    # z coordinates of the slab: the same LinRange nodes as the full grid's first planes,
+    # which only changes vertex positions, not the work done
+    rng = ((0, 1), (0, 1), (0, 1))
+    for _ in range(warmup):
+        oracle.isosurface(A, 'mc', np.float32(0), 1e-3, rng)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        v, f = oracle.isosurface(A, 'mc', np.float32(0), 1e-3, rng)
+    dt = (time.perf_counter() - t0) / steps
+    vox = float(n) * n * (planes + 1)
+    return vox / dt / 1e9, dt, len(v), len(f), vox
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    planes = args.cpu_planes
+    val, dt, nv, nf, vox = cpu_baseline(args.n, planes, steps=args.steps, warmup=args.warmup)
+    sample = ('z slab %dx%dx%d (%.0f M samples) of the benchmark field, CPU restatement of MarchingCubes '
+              '(oracle/oracle.c, single-threaded like Meshing.jl), %.2f s per step' %
+              (args.n, args.n, planes + 1, vox / 1e6, dt))
+    line = {'impl': 'reference', 'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes',
+            'value': val, 'unit': 'Gvoxels/s', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': dt * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD % args.n, 'sample_planes': planes + 1},
+            'cpu_baseline': {'value': val, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port', 'sample': sample},
+            'e2e': {'value': val, 'unit': 'Gvoxels/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    lib = pkg.load_library()
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    n = args.n
+    vol = sines_device(n, device=dev)
+    torch.cuda.synchronize()
+    m = pkg.MarchingCubes(iso=np.float32(0))
+    X = Y = Z = (0, 1)
+    ctx = pkg.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    p = pkg.make_params(m, X, Y, Z)
+    nv, nf = ctypes.c_int64(), ctypes.c_int64()
+    pkg._lib.check(lib.mesh_count(ctx.handle, ctypes.c_void_p(vol.data_ptr()), 2, n, n, n, 1, ctypes.byref(p),
+                                  ctypes.byref(nv), ctypes.byref(nf)), ctx.handle)
+    nv, nf = nv.value, nf.value
+    verts = torch.empty((nv, 3), dtype=torch.float32, device=dev)
+    faces = torch.empty((nf, 3), dtype=torch.int64, device=dev)
+    counts = torch.zeros(2, dtype=torch.int64, device=dev)
+
+    def step():
+        pkg._lib.check(lib.mesh_extract_device(ctx.handle, ctypes.c_void_p(vol.data_ptr()), 2, n, n, n,
+                                               ctypes.byref(p), ctypes.c_void_p(verts.data_ptr()), nv,
+                                               ctypes.c_void_p(faces.data_ptr()), nf,
+                                               ctypes.c_void_p(counts.data_ptr())), ctx.handle)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    ctx.stage_times()  # reset
+    ctx.enable_timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local) if rank == 0 else None
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop() if clocks else None
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    st = ctx.stage_times()
+    ctx.enable_timing(False)
+    assert counts.tolist() == [nv, nf]
+
+    # end to end through the drop-in C ABI with pinned host buffers
+    hvol = torch.empty((n, n, n), dtype=torch.float32, pin_memory=True)
+    hvol.copy_(vol.permute(2, 1, 0))
+    hv = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
+    hf = torch.empty((nf, 3), dtype=torch.int64, pin_memory=True)
+    ctx.set_stream(None)
+
+    def e2e_step():
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        pkg._lib.check(lib.mesh_count(ctx.handle, ctypes.c_void_p(hvol.data_ptr()), 2, n, n, n, 0, ctypes.byref(p),
+                                      ctypes.byref(a), ctypes.byref(b)), ctx.handle)
+        pkg._lib.check(lib.mesh_fill(ctx.handle, ctypes.c_void_p(hv.data_ptr()), ctypes.c_void_p(hf.data_ptr()), 0),
+                       ctx.handle)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    ok = torch.equal(hv.to(dev), verts) and torch.equal(hf.to(dev), faces)
+
+    if dist:
+        t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = t.tolist()
+    if rank != 0:
+        return
+    vox = float(n) ** 3
+    peak, peak_kind = measured_peak()
+    in_b = vox * 4
+    out_b = nv * 12 + nf * 24
+    stage = {k: v[0] / max(v[1], 1) for k, v in st.items()}
+    # algorithmic bytes per launch: classify reads the volume once; emit writes the mesh
+    alg_bytes = {'classify': in_b, 'scan': (n - 1) ** 2 * 2 * (4 + 8) * 1.0, 'emit': out_b}
+    dom = max(stage, key=stage.get)
+    achieved = alg_bytes[dom] / (stage[dom] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, 'profiles', 'traffic.json')
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get('%s_%d' % (dom, n))
+        except ValueError:
+            traffic = None
+    pipe_gbs = (in_b + out_b) / (ms * 1e-3) / 1e9
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cval, cdt, _, _, cvox = cpu_baseline(n, args.cpu_planes)
+        cpu = {'value': cval, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port',
+               'sample': 'z slab %dx%dx%d of the same field, CPU restatement of MarchingCubes (oracle/oracle.c, '
+                         'single-threaded like Meshing.jl), %.2f s' % (n, n, args.cpu_planes + 1, cdt)}
+    line = {
+        'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes',
+        'value': vox * world / (ms * 1e-3) / 1e9,
+        'unit': 'Gvoxels/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+        'config': {'workload': WORKLOAD % n, 'nx': n, 'ny': n, 'nz': n, 'cells': (n - 1) ** 3, 'nverts': nv,
+                   'nfaces': nf, 'output': 'Float32 vertices, Int64 1-based faces', 'l2': 'inputs larger than L2',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU',
+                   'stage_ms': stage, 'e2e_matches_device': bool(ok)},
+        'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': traffic, 'peak_source': peak_kind,
+                     'algorithmic_bytes': alg_bytes[dom]},
+        'pipeline': {'bytes': in_b + out_b, 'achieved': pipe_gbs, 'frac': pipe_gbs / peak, 'unit': 'GB/s'},
+        'e2e': {'value': vox * world / (e2e_ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': e2e_ms,
+                'h2d_bytes_per_step': int(in_b), 'd2h_bytes_per_step': int(out_b)},
+        'gpu_launches': int(sum(v[1] for v in st.values())),
+        'cpu_baseline': cpu,
+        'clocks': ck,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--n', type=int, default=N_DEFAULT, help='grid size per axis (default 1024)')
+    ap.add_argument('--cpu-planes', type=int, default=128, help='z planes of the CPU sample')
+    ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    args = ap.parse_args()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    import __graft_entry__ as ge
+    ge.load_package()
+    if args.impl == 'reference':
+        run_reference(args, rank, world)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+        tdist.init_process_group('nccl')
+        dist = tdist
+    try:
+        run_ours(args, rank, world, dist)
+    finally:
+        if dist:
+            dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

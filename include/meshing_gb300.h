@@ -1,0 +1,128 @@
+/*
+ * meshing_gb300.h -- C ABI of the GB300 isosurface engine.
+ *
+ * Drop-in device back end for Meshing.jl's `isosurface(A, alg, X, Y, Z)`:
+ *   - MarchingCubes       replaces src/marching_cubes.jl:27-64 (with :67-120)
+ *   - MarchingTetrahedra  replaces src/marching_tetrahedra.jl:129-163 (with :11-127)
+ *   - NaiveSurfaceNets    named by the reference (README.md:21) but not
+ *                         implemented there; defined by this project.
+ * The algorithm structs (src/algorithmtypes.jl:23-25,37-40) map onto
+ * `mesh_params`; the generic forwarder `isosurface(A, args...)`
+ * (src/isosurface.jl:30-32) stays on the Julia side.
+ *
+ * Results are those of the reference: vertices `NTuple{3, float(FT)}` with
+ * FT = promote_type(eltype(first(X)), eltype(first(Y)), eltype(first(Z)),
+ * eltype(A), typeof(iso)[, typeof(eps)]), faces `NTuple{3, Int}` with 1-based
+ * indices, both in the reference's emission order.
+ *
+ * The volume uses Julia's column-major layout: A[x, y, z] is element
+ * x + nx*(y + ny*z) (0-based).  No function throws; every function returns a
+ * `mesh_status`.  A context is not thread-safe; use one context per thread.
+ */
+#ifndef MESHING_GB300_H
+#define MESHING_GB300_H
+
+#include <stdint.h>
+
+#ifndef MESH_API
+#define MESH_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Element types (volume, iso, eps, range endpoints). */
+typedef enum {
+    MESH_DT_U16 = 1, /* UInt16 */
+    MESH_DT_F32 = 2, /* Float32 */
+    MESH_DT_F64 = 3, /* Float64 */
+    MESH_DT_I64 = 4  /* Int64 (iso and range endpoints only) */
+} mesh_dtype;
+
+typedef enum {
+    MESH_ALG_MC = 0,  /* MarchingCubes       (src/algorithmtypes.jl:23-25) */
+    MESH_ALG_MT = 1,  /* MarchingTetrahedra  (src/algorithmtypes.jl:37-40) */
+    MESH_ALG_NSN = 2  /* NaiveSurfaceNets    (defined by this project) */
+} mesh_alg;
+
+typedef enum {
+    MESH_OK = 0,
+    MESH_EINVAL = 1,       /* bad argument (null pointer, unsupported type, non-finite range, ...) */
+    MESH_ENOMEM = 2,       /* device or pinned-host allocation failed */
+    MESH_ECUDA = 3,        /* a CUDA runtime call failed */
+    MESH_EDEVICE = 4,      /* a kernel reported an error (bounded wait expired, bounds check) */
+    MESH_ESTATE = 5,       /* mesh_fill without a preceding successful mesh_count */
+    MESH_ECAPACITY = 6,    /* output buffers smaller than the mesh */
+    MESH_ETOOLARGE = 7     /* volume beyond the engine's index limits */
+} mesh_status;
+
+/* Mirrors MarchingCubes{T}(iso) / MarchingTetrahedra{T,E}(iso, eps) plus the
+ * X, Y, Z arguments of isosurface.  Each scalar travels as a double together
+ * with its Julia type; Int64 values must satisfy |v| <= 2^53. */
+typedef struct {
+    int32_t alg;        /* mesh_alg */
+    int32_t iso_type;   /* MESH_DT_F32 | MESH_DT_F64 | MESH_DT_I64 */
+    double iso;
+    int32_t eps_type;   /* MESH_DT_F32 | MESH_DT_F64 (MT only; ignored otherwise) */
+    double eps;
+    int32_t range_type; /* eltype of first(X) == first(Y) == first(Z): MESH_DT_I64 | F32 | F64 */
+    double range[6];    /* first(X), last(X), first(Y), last(Y), first(Z), last(Z) */
+} mesh_params;
+
+/* Fills `p` with the reference defaults: MarchingCubes(iso=0.0), eps=1e-3,
+ * X = Y = Z = -1:1 (src/algorithmtypes.jl:23-25,37-40; src/marching_cubes.jl:27). */
+MESH_API void mesh_params_default(mesh_params *p);
+
+typedef struct mesh_ctx mesh_ctx;
+
+/* Creates a context bound to CUDA device `device` with its own stream. */
+MESH_API int mesh_ctx_create(int device, mesh_ctx **out);
+MESH_API void mesh_ctx_destroy(mesh_ctx *ctx);
+/* Makes the context issue its work on `stream` (a cudaStream_t; NULL = the context's own). */
+MESH_API int mesh_ctx_set_stream(mesh_ctx *ctx, void *stream);
+MESH_API const char *mesh_status_string(int status);
+/* Last error message recorded on `ctx` (empty string if none). */
+MESH_API const char *mesh_ctx_last_error(const mesh_ctx *ctx);
+
+/* Bits (32 or 64) of float(FT) for a volume of `vol_dtype` under `p`. */
+MESH_API int mesh_output_float_bits(int vol_dtype, const mesh_params *p, int *bits);
+
+/* Phase 1 of the two-phase drop-in call (replaces the loops of
+ * src/marching_cubes.jl:40-63 / src/marching_tetrahedra.jl:144-160):
+ * classifies every cell and scans the per-column counts.  `vol` is a host
+ * pointer (vol_on_device = 0, copied in by the library) or a device pointer
+ * (vol_on_device = 1, must stay valid until mesh_fill returns).  Blocks until
+ * the counts are known. */
+MESH_API int mesh_count(mesh_ctx *ctx, const void *vol, int vol_dtype, int64_t nx, int64_t ny, int64_t nz,
+               int vol_on_device, const mesh_params *p, int64_t *nverts, int64_t *nfaces);
+
+/* Phase 2: writes exactly nverts*3 floats (float or double, per
+ * mesh_output_float_bits) to `verts` and nfaces*3 int64 (1-based) to `faces`,
+ * host pointers (out_on_device = 0) or device pointers (1).  Blocks until done. */
+MESH_API int mesh_fill(mesh_ctx *ctx, void *verts, int64_t *faces, int out_on_device);
+
+/* Device-resident single call, asynchronous on the context stream: classify,
+ * scan and emit with no host round trip.  `vol`, `verts`, `faces` and
+ * `counts` are device pointers; counts[0] = nverts and counts[1] = nfaces are
+ * written on the device.  If the mesh exceeds verts_cap / faces_cap nothing
+ * beyond the capacities is written and mesh_ctx_sync() returns MESH_ECAPACITY;
+ * counts still hold the true sizes. */
+MESH_API int mesh_extract_device(mesh_ctx *ctx, const void *vol, int vol_dtype, int64_t nx, int64_t ny, int64_t nz,
+                        const mesh_params *p, void *verts, int64_t verts_cap, int64_t *faces, int64_t faces_cap,
+                        int64_t *counts);
+/* Waits for the context's outstanding work and reports device-side errors. */
+MESH_API int mesh_ctx_sync(mesh_ctx *ctx);
+
+/* Diagnostics (no counterpart in the reference, which has no instrumentation):
+ * with timing enabled the context brackets every classify, scan and emit
+ * launch with CUDA events on its stream.  mesh_ctx_stage_times waits for them
+ * and returns, per stage, the summed device milliseconds (ms[0..2]) and the
+ * number of launches (launches[0..2]) since the previous query, then resets. */
+MESH_API int mesh_ctx_enable_timing(mesh_ctx *ctx, int enable);
+MESH_API int mesh_ctx_stage_times(mesh_ctx *ctx, double *ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MESHING_GB300_H */

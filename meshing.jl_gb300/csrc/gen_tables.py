@@ -179,6 +179,10 @@ def emit(out, mc, mt_t, mt):
     w('// and procVox (src/marching_tetrahedra.jl:105-127).')
     w('#pragma once')
     w('#include <stdint.h>')
+    w('// Storage class of the tables; device code defines it as `static __device__ const`.')
+    w('#ifndef MESH_TBL')
+    w('#define MESH_TBL static const')
+    w('#endif')
     w('')
     w('// ---- Marching Cubes (corner order of src/marching_cubes.jl:42-49) ----')
     w('// MC_CASE_VERTS[c]: nibble k (bits 4k..4k+3) = cube edge (0..11) of local vertex slot k;')
@@ -203,11 +207,11 @@ def emit(out, mc, mt_t, mt):
         maxnf = max(maxnf, len(faces))
     w('#define MC_MAX_VERTS %d' % maxnv)
     w('#define MC_MAX_FACES %d' % maxnf)
-    w('static const uint64_t MC_CASE_VERTS[256] = {')
+    w('MESH_TBL uint64_t MC_CASE_VERTS[256] = {')
     for i in range(0, 256, 4):
         w('  ' + ', '.join('0x%016xull' % x for x in vw[i:i + 4]) + ',')
     w('};')
-    w('static const uint64_t MC_CASE_FACES[256] = {')
+    w('MESH_TBL uint64_t MC_CASE_FACES[256] = {')
     for i in range(0, 256, 4):
         w('  ' + ', '.join('0x%016xull' % x for x in fw[i:i + 4]) + ',')
     w('};')
@@ -228,32 +232,41 @@ def emit(out, mc, mt_t, mt):
     maxt = max(len(o) for o in orders)
     w('#define MT_MAX_FACES %d' % maxf)
     w('#define MT_MAX_TOUCH %d' % maxt)
-    w('static const uint8_t MT_CASE_NFACES[256] = {')
+    w('MESH_TBL uint8_t MT_CASE_NFACES[256] = {')
     for i in range(0, 256, 16):
         w('  ' + ', '.join('%d' % len(mt[c]) for c in range(i, i + 16)) + ',')
     w('};')
-    w('static const uint8_t MT_CASE_FACES[256][%d] = {' % (3 * maxf))
+    w('MESH_TBL uint8_t MT_CASE_FACES[256][%d] = {' % (3 * maxf))
     for c in range(256):
         flat = [e for f in mt[c] for e in f]
         flat += [0xff] * (3 * maxf - len(flat))
         w('  {' + ','.join('%d' % e for e in flat) + '},')
     w('};')
-    w('static const uint32_t MT_TOUCHED[256] = {')
+    w('MESH_TBL uint32_t MT_TOUCHED[256] = {')
     for i in range(0, 256, 8):
         w('  ' + ', '.join('0x%05xu' % sum(1 << e for e in orders[c]) for c in range(i, i + 8)) + ',')
     w('};')
-    w('static const uint8_t MT_TOUCH_ORDER[256][%d] = {' % maxt)
+    w('MESH_TBL uint8_t MT_TOUCH_ORDER[256][%d] = {' % maxt)
     for c in range(256):
         o = orders[c] + [0xff] * (maxt - len(orders[c]))
         w('  {' + ','.join('%d' % e for e in o) + '},')
     w('};')
+    w('// MT_BEFORE[c][e]: mask of the edges first used before edge e in case c (0 if e is unused).')
+    w('MESH_TBL uint32_t MT_BEFORE[256][19] = {')
+    for c in range(256):
+        o = orders[c]
+        row = []
+        for e in range(19):
+            row.append(sum(1 << x for x in o[:o.index(e)]) if e in o else 0)
+        w('  {' + ','.join('0x%05xu' % m for m in row) + '},')
+    w('};')
     w('')
     w('// Voxel geometry restated from src/lut/mt.jl:23-56 (0-based corners).')
-    w('static const uint8_t MT_CORNER_POS[8][3] = {' +
+    w('MESH_TBL uint8_t MT_CORNER_POS[8][3] = {' +
       ', '.join('{%d,%d,%d}' % tuple(p) for p in mt_t['voxCrnrPos']) + '};')
-    w('static const uint8_t MT_EDGE_CORNERS[19][2] = {' +
+    w('MESH_TBL uint8_t MT_EDGE_CORNERS[19][2] = {' +
       ', '.join('{%d,%d}' % (a - 1, b - 1) for a, b in mt_t['voxEdgeCrnrs']) + '};')
-    w('static const uint8_t MT_EDGE_DIR[19] = {' + ', '.join('%d' % d for d in mt_t['voxEdgeDir']) + '};')
+    w('MESH_TBL uint8_t MT_EDGE_DIR[19] = {' + ', '.join('%d' % d for d in mt_t['voxEdgeDir']) + '};')
     w('')
     open(out, 'w').write('\n'.join(L) + '\n')
 

@@ -1,0 +1,157 @@
+// K2 -- scan: exclusive prefix of the per-piece counts in the reference's
+// emission order.
+//
+// The reference numbers vertices and faces by `push!` order, i.e. cells in
+// lexicographic (x, y, z) order with z fastest (src/marching_cubes.jl:40,
+// src/marching_tetrahedra.jl:144).  A piece (x, y, seg) is a z segment of one
+// column, so the emission order of pieces is (x, y, seg) lexicographic, while
+// the counts sit in memory as [seg][y][x] (x fastest, written coalesced by
+// the classify kernel).
+//
+// One CTA scans 32 columns (lane = x, so every access stays coalesced): its
+// 32 warps split the (y, seg) sequence of every column, reduce, scan across
+// warps through shared memory, scan the 32 column totals with warp shuffles,
+// and chain the groups of 32 columns with a single-pass decoupled look-back
+// (groups are taken in ticket order, so every predecessor is already
+// resident).  Look-back waits are bounded: on expiry the kernel sets
+// ERR_SCAN_TIMEOUT in the device error word and finishes without hanging.
+#include "mesh_internal.cuh"
+
+namespace mesh {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr unsigned long long FLAG_AGG = 1ull << 62;
+constexpr unsigned long long FLAG_INC = 2ull << 62;
+constexpr unsigned long long VAL_MASK = (1ull << 62) - 1;
+
+__device__ __forceinline__ void st_release(unsigned long long *a, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *a) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+    return v;
+}
+
+// Exclusive prefix of tile `tile` for one counter, given its aggregate.
+__device__ int64_t look_back(unsigned long long *state, int tile, int64_t agg, int spin_limit, unsigned *err) {
+    if (tile == 0) {
+        st_release(&state[0], FLAG_INC | (unsigned long long)agg);
+        return 0;
+    }
+    st_release(&state[tile], FLAG_AGG | (unsigned long long)agg);
+    int64_t excl = 0;
+    int k = tile - 1;
+    int spins = 0;
+    while (k >= 0) {
+        const unsigned long long w = ld_acquire(&state[k]);
+        const unsigned long long f = w & ~VAL_MASK;
+        if (f == 0) {
+            if (++spins > spin_limit) {
+                atomicOr(err, ERR_SCAN_TIMEOUT);
+                break;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        excl += (int64_t)(w & VAL_MASK);
+        if (f == FLAG_INC) break;
+        k--;
+    }
+    st_release(&state[tile], FLAG_INC | (unsigned long long)(excl + agg));
+    return excl;
+}
+
+__global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
+    __shared__ int s_tile;
+    __shared__ int64_t s_part[2][32][33];
+    __shared__ int64_t s_xpre[2][32];
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.scan_ticket, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int x = tile * 32 + lane;
+    const bool xok = x < p.cx;
+    const int64_t L = (int64_t)p.cy * p.nseg;
+    const int64_t per = (L + 31) / 32;
+    const int64_t j0 = min(L, (int64_t)w * per), j1 = min(L, j0 + per);
+    const int64_t np = npieces(p);
+
+    int64_t sv = 0, sf = 0;
+    if (xok) {
+        int y = (int)(j0 / p.nseg), seg = (int)(j0 % p.nseg);
+        for (int64_t j = j0; j < j1; j++) {
+            const int64_t i = piece(p, seg, y, x);
+            sv += p.cnt[i];
+            sf += p.cnt[np + i];
+            if (++seg == p.nseg) { seg = 0; ++y; }
+        }
+    }
+    s_part[0][w][lane] = sv;
+    s_part[1][w][lane] = sf;
+    __syncthreads();
+
+    if (w == 0) {
+        int64_t tv = 0, tf = 0;  // column totals; s_part becomes the per-warp exclusive prefix
+        for (int k = 0; k < 32; k++) {
+            const int64_t a = s_part[0][k][lane], b = s_part[1][k][lane];
+            s_part[0][k][lane] = tv;
+            s_part[1][k][lane] = tf;
+            tv += a;
+            tf += b;
+        }
+        int64_t iv = tv, jf = tf;  // inclusive scan across the 32 columns
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t a = __shfl_up_sync(FULL, iv, o), b = __shfl_up_sync(FULL, jf, o);
+            if (lane >= o) { iv += a; jf += b; }
+        }
+        const int64_t aggv = __shfl_sync(FULL, iv, 31), aggf = __shfl_sync(FULL, jf, 31);
+        int64_t pv = 0, pf = 0;
+        if (lane == 0) {
+            pv = look_back(p.scan_state, tile, aggv, p.scan_spin_limit, p.err);
+            pf = look_back(p.scan_state + ntiles, tile, aggf, p.scan_spin_limit, p.err);
+            if (tile == ntiles - 1) {
+                p.totals[0] = pv + aggv;
+                p.totals[1] = pf + aggf;
+            }
+        }
+        pv = __shfl_sync(FULL, pv, 0);
+        pf = __shfl_sync(FULL, pf, 0);
+        s_xpre[0][lane] = pv + iv - tv;
+        s_xpre[1][lane] = pf + jf - tf;
+    }
+    __syncthreads();
+
+    if (xok) {
+        int64_t bv = s_xpre[0][lane] + s_part[0][w][lane];
+        int64_t bf = s_xpre[1][lane] + s_part[1][w][lane];
+        int y = (int)(j0 / p.nseg), seg = (int)(j0 % p.nseg);
+        for (int64_t j = j0; j < j1; j++) {
+            const int64_t i = piece(p, seg, y, x);
+            p.base[i] = bv;
+            p.base[np + i] = bf;
+            bv += p.cnt[i];
+            bf += p.cnt[np + i];
+            if (++seg == p.nseg) { seg = 0; ++y; }
+        }
+    }
+}
+
+}  // namespace
+
+int scan_tiles(const Plan &p) { return (p.cx + 31) / 32; }
+
+cudaError_t launch_scan(const Plan &p, cudaStream_t s) {
+    const int ntiles = scan_tiles(p);
+    cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * 2 * (size_t)ntiles, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(p.scan_ticket, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    k_scan<<<ntiles, 1024, 0, s>>>(p, ntiles);
+    return cudaGetLastError();
+}
+
+}  // namespace mesh

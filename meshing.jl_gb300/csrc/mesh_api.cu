@@ -1,0 +1,581 @@
+// Host runtime behind the C ABI (include/meshing_gb300.h).
+//
+// Turns a reference call isosurface(A, alg, X, Y, Z) into a launch plan:
+// Julia's type promotion (src/marching_cubes.jl:31, src/marching_tetrahedra.jl:131)
+// picks the arithmetic and output types, the LinRange node coordinates
+// (src/marching_cubes.jl:36-38) are tabulated once per call on the host with
+// the exact Base.lerpi arithmetic, and the three kernels run on the context's
+// stream: classify -> scan -> emit.  Device scratch grows monotonically and is
+// reused across calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mesh_internal.cuh"
+#include "mesh_tables.h"
+
+namespace mesh {
+cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, cudaStream_t s);
+cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
+int scan_tiles(const Plan &p);
+}  // namespace mesh
+
+using namespace mesh;
+
+namespace {
+
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        size_t want = std::max(n, cap + cap / 4);
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            e = cudaMalloc(&ptr, n);
+            if (e != cudaSuccess) return e;
+            want = n;
+        }
+        cap = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct mesh_ctx {
+    int device = 0;
+    int sms = 148;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f;
+    int64_t *h_misc = nullptr;  // pinned: totals[2], err
+    Plan plan{};
+    int have_plan = 0;
+    int Q64 = 0, A64 = 0, P64 = 0;
+    int64_t nverts = 0, nfaces = 0;
+    std::string msg;
+    // stage timing (diagnostics)
+    int timing = 0;
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<cudaEvent_t> ev_pairs[3];  // start, stop, start, stop, ...
+};
+
+namespace {
+
+constexpr double EXACT_INT = 9007199254740992.0;  // 2^53
+
+int fail(mesh_ctx *c, int status, const char *fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        c->msg = buf;
+    }
+    return status;
+}
+
+int cuda_fail(mesh_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(c, MESH_ENOMEM, "%s: %s", what, cudaGetErrorString(e));
+    }
+    return fail(c, MESH_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+bool is_f32_exact(double v) { return std::isnan(v) || (double)(float)v == v; }
+
+bool valid_scalar(int ty, double v) {
+    switch (ty) {
+    case MESH_DT_F64: return true;
+    case MESH_DT_F32: return is_f32_exact(v);
+    case MESH_DT_I64: return std::isfinite(v) && std::floor(v) == v && std::fabs(v) <= EXACT_INT;
+    default: return false;
+    }
+}
+
+// float(FT) is Float64 unless some participating type is Float32 and none is Float64.
+int out_is_f64(const int *tys, int n) {
+    int any32 = 0;
+    for (int i = 0; i < n; i++) {
+        if (tys[i] == MESH_DT_F64) return 1;
+        if (tys[i] == MESH_DT_F32) any32 = 1;
+    }
+    return any32 ? 0 : 1;
+}
+
+int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_params *p) {
+    if (!p) return fail(c, MESH_EINVAL, "params is NULL");
+    if (T != MESH_DT_U16 && T != MESH_DT_F32 && T != MESH_DT_F64)
+        return fail(c, MESH_EINVAL, "unsupported volume dtype %d", T);
+    if (p->alg != MESH_ALG_MC && p->alg != MESH_ALG_MT && p->alg != MESH_ALG_NSN)
+        return fail(c, MESH_EINVAL, "unknown algorithm %d", p->alg);
+    if (p->iso_type != MESH_DT_F32 && p->iso_type != MESH_DT_F64 && p->iso_type != MESH_DT_I64)
+        return fail(c, MESH_EINVAL, "unsupported iso type %d", p->iso_type);
+    if (!valid_scalar(p->iso_type, p->iso)) return fail(c, MESH_EINVAL, "iso value not representable in its type");
+    if (p->alg == MESH_ALG_MT) {
+        if (p->eps_type != MESH_DT_F32 && p->eps_type != MESH_DT_F64)
+            return fail(c, MESH_EINVAL, "unsupported eps type %d", p->eps_type);
+        if (!valid_scalar(p->eps_type, p->eps)) return fail(c, MESH_EINVAL, "eps value not representable in its type");
+    }
+    if (p->range_type != MESH_DT_F32 && p->range_type != MESH_DT_F64 && p->range_type != MESH_DT_I64)
+        return fail(c, MESH_EINVAL, "unsupported range type %d", p->range_type);
+    for (int i = 0; i < 6; i++) {
+        if (!std::isfinite(p->range[i])) return fail(c, MESH_EINVAL, "range endpoints must be finite");
+        if (!valid_scalar(p->range_type, p->range[i])) return fail(c, MESH_EINVAL, "range endpoint not representable");
+    }
+    if (nx < 0 || ny < 0 || nz < 0) return fail(c, MESH_EINVAL, "negative dimension");
+    const int64_t lim = (int64_t)1 << 30;
+    if (nx > lim || ny > lim || nz > lim) return fail(c, MESH_ETOOLARGE, "dimension above 2^30");
+    return MESH_OK;
+}
+
+// LinRange(a, b, n) in eltype L (Base.lerpi): T((1-t)*a + t*b), t = i/(n-1).
+void linrange(int L32, double a, double b, int64_t n, double *out) {
+    const double aa = L32 ? (double)(float)a : a, bb = L32 ? (double)(float)b : b;
+    const int64_t d = n > 1 ? n - 1 : 1;
+    for (int64_t i = 0; i < n; i++) {
+        const double t = (double)i / (double)d;
+        const double v = (1.0 - t) * aa + t * bb;
+        out[i] = L32 ? (double)(float)v : v;
+    }
+}
+
+void own_masks(uint32_t own[8]) {
+    for (int bnd = 0; bnd < 8; bnd++) {
+        uint32_t m = 0;
+        for (int e = 0; e < 19; e++) {
+            const int i1 = MT_EDGE_CORNERS[e][0], i2 = MT_EDGE_CORNERS[e][1];
+            int za = 0;
+            for (int k = 0; k < 3; k++)
+                if (MT_CORNER_POS[i1][k] == 0 && MT_CORNER_POS[i2][k] == 0) za |= 1 << k;
+            if ((za & ~bnd) == 0) m |= 1u << e;
+        }
+        own[bnd] = m;
+    }
+}
+
+int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
+            const mesh_params *p) {
+    Plan &P = c->plan;
+    P = Plan{};
+    c->have_plan = 0;
+    P.nx = nx; P.ny = ny; P.nz = nz;
+    P.cx = (int32_t)(nx - 1); P.cy = (int32_t)(ny - 1); P.cz = (int32_t)(nz - 1);
+    P.T = T;
+    P.alg = p->alg;
+    const int I = p->iso_type, E = p->eps_type, Rt = p->range_type;
+    const int mt = p->alg == MESH_ALG_MT;
+    c->Q64 = T == MESH_DT_F64 || I == MESH_DT_F64 || (T == MESH_DT_U16 && I == MESH_DT_I64);
+    const int L32 = Rt == MESH_DT_F32;
+    c->A64 = mt ? (c->Q64 || E == MESH_DT_F64) : c->Q64;
+    c->P64 = c->A64 || !L32;
+    if (!mt) c->P64 = c->Q64 || !L32;
+    const int tys[4] = {Rt, T, I, E};
+    P.out64 = out_is_f64(tys, mt ? 4 : 3);
+
+    const double iso = p->iso;
+    // thresholds: v < iso  <=>  v < thr in the data type
+    {
+        float f = (float)iso;
+        if (!std::isnan(iso) && (double)f < iso) f = std::nextafter(f, INFINITY);
+        P.thr_f = f;
+        P.thr_d = iso;
+        double ce = std::ceil(iso);
+        if (std::isnan(iso)) ce = 0;
+        P.thr_i = (int32_t)std::min(65536.0, std::max(0.0, ce));
+    }
+    P.isoq_d = iso;
+    P.isoq_f = (float)iso;
+    if (mt) {
+        const int te64 = T == MESH_DT_F64 || E == MESH_DT_F64;  // promote(T, E)
+        const double hi = te64 ? 1.0 - p->eps : (double)(1.0f - (float)p->eps);
+        P.eps_d = p->eps;
+        P.hi_d = hi;
+        P.eps_f = (float)p->eps;
+        P.hi_f = (float)hi;
+        own_masks(P.own);
+    }
+
+    // tiling
+    P.tiles_x = (P.cx + TILE_X - 1) / TILE_X;
+    P.tiles_y = (P.cy + WY - 1) / WY;
+    const int64_t per_seg = (int64_t)P.tiles_x * P.tiles_y;
+    const int64_t target = (int64_t)c->sms * 64;
+    const int maxseg = (P.cz + ZC - 1) / ZC;
+    int nseg = (int)std::min<int64_t>(maxseg, std::max<int64_t>(1, (target + per_seg - 1) / per_seg));
+    int zs = (P.cz + nseg - 1) / nseg;
+    zs = (zs + ZC - 1) / ZC * ZC;
+    P.zs = zs;
+    P.nseg = (P.cz + zs - 1) / zs;
+    P.chunks_per_seg = zs / ZC;
+    P.nchunks = P.nseg * P.chunks_per_seg;
+    if ((P.tiles_y + WARPS - 1) / WARPS > 65535 || P.nseg > 65535)
+        return fail(c, MESH_ETOOLARGE, "grid too large for this volume shape");
+
+    cudaError_t e;
+    const size_t es = T == MESH_DT_U16 ? 2 : T == MESH_DT_F32 ? 4 : 8;
+    const size_t vbytes = (size_t)nx * ny * nz * es;
+    if (vol_on_device) {
+        P.vol = vol;
+    } else {
+        if ((e = c->vol.ensure(vbytes)) != cudaSuccess) return cuda_fail(c, e, "volume buffer");
+        if ((e = cudaMemcpyAsync(c->vol.ptr, vol, vbytes, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
+            return cuda_fail(c, e, "volume upload");
+        P.vol = c->vol.ptr;
+    }
+
+    // coordinate tables: xp yp zp dx dy dz (double) then the same as float
+    const int64_t ntab = nx + ny + nz;
+    const size_t tbytes = (size_t)ntab * 2 * (sizeof(double) + sizeof(float));
+    double *h = (double *)malloc(tbytes);
+    if (!h) return fail(c, MESH_ENOMEM, "host table buffer");
+    double *hp = h, *hd = h + ntab;
+    float *hpf = (float *)(h + 2 * ntab), *hdf = hpf + ntab;
+    const int64_t ns[3] = {nx, ny, nz};
+    int64_t off = 0;
+    for (int a = 0; a < 3; a++) {
+        linrange(L32, p->range[2 * a], p->range[2 * a + 1], ns[a], hp + off);
+        for (int64_t i = 0; i < ns[a]; i++) {
+            double d = 0;
+            if (i + 1 < ns[a]) {
+                d = hp[off + i + 1] - hp[off + i];
+                if (L32) d = (double)((float)hp[off + i + 1] - (float)hp[off + i]);
+            }
+            hd[off + i] = d;
+            hpf[off + i] = (float)hp[off + i];
+            hdf[off + i] = (float)d;
+        }
+        off += ns[a];
+    }
+    if ((e = c->tabs.ensure(tbytes)) != cudaSuccess) { free(h); return cuda_fail(c, e, "table buffer"); }
+    e = cudaMemcpyAsync(c->tabs.ptr, h, tbytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // h is pageable and freed below
+    free(h);
+    if (e != cudaSuccess) return cuda_fail(c, e, "table upload");
+    double *dp = (double *)c->tabs.ptr;
+    P.xp = dp; P.yp = dp + nx; P.zp = dp + nx + ny;
+    P.dx = dp + ntab; P.dy = P.dx + nx; P.dz = P.dx + nx + ny;
+    float *fp = (float *)(dp + 2 * ntab);
+    P.xpf = fp; P.ypf = fp + nx; P.zpf = fp + nx + ny;
+    P.dxf = fp + ntab; P.dyf = P.dxf + nx; P.dzf = P.dxf + nx + ny;
+
+    // scratch
+    const int64_t np = npieces(P);
+    if ((e = c->cnt.ensure((size_t)np * 2 * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(c, e, "count buffer");
+    if ((e = c->base.ensure((size_t)np * 2 * sizeof(int64_t))) != cudaSuccess) return cuda_fail(c, e, "base buffer");
+    const size_t fb = (size_t)P.nchunks * P.tiles_x * P.cy;
+    if ((e = c->flags.ensure(fb)) != cudaSuccess) return cuda_fail(c, e, "flag buffer");
+    const int st = scan_tiles(P);
+    if ((e = c->scan.ensure((size_t)st * 2 * sizeof(unsigned long long) + 64)) != cudaSuccess)
+        return cuda_fail(c, e, "scan buffer");
+    P.cnt = (uint32_t *)c->cnt.ptr;
+    P.base = (int64_t *)c->base.ptr;
+    P.flags = (uint8_t *)c->flags.ptr;
+    P.scan_state = (unsigned long long *)c->scan.ptr;
+    P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + (size_t)st * 2 * sizeof(unsigned long long));
+    P.totals = (int64_t *)c->misc.ptr;
+    P.err = (unsigned int *)((int64_t *)c->misc.ptr + 2);
+    P.scan_spin_limit = 1 << 24;
+    return MESH_OK;
+}
+
+cudaEvent_t take_event(mesh_ctx *c) {
+    if (!c->ev_free.empty()) {
+        cudaEvent_t e = c->ev_free.back();
+        c->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+void mark(mesh_ctx *c, int stage) {
+    if (!c->timing) return;
+    cudaEvent_t e = take_event(c);
+    if (!e) return;
+    cudaEventRecord(e, c->stream);
+    c->ev_pairs[stage].push_back(e);
+}
+
+int run_count(mesh_ctx *c) {
+    Plan &P = c->plan;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(c->misc.ptr, 0, 32, c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
+    mark(c, 0);
+    if ((e = launch_classify(P, c->stream)) != cudaSuccess) return cuda_fail(c, e, "classify launch");
+    mark(c, 0);
+    mark(c, 1);
+    if ((e = launch_scan(P, c->stream)) != cudaSuccess) return cuda_fail(c, e, "scan launch");
+    mark(c, 1);
+    return MESH_OK;
+}
+
+int check_err(mesh_ctx *c) {
+    const unsigned err = (unsigned)c->h_misc[2];
+    if (err & ERR_SCAN_TIMEOUT) return fail(c, MESH_EDEVICE, "scan look-back wait expired");
+    if (err & ERR_BOUNDS) return fail(c, MESH_EDEVICE, "device bounds check failed");
+    if (err & ERR_CAPACITY) return fail(c, MESH_ECAPACITY, "output capacity too small");
+    return MESH_OK;
+}
+
+int fetch_misc(mesh_ctx *c) {
+    cudaError_t e = cudaMemcpyAsync(c->h_misc, c->misc.ptr, 3 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "synchronize");
+    c->h_misc[2] &= 0xffffffffll;
+    return MESH_OK;
+}
+
+int launch_emit(mesh_ctx *c) {
+    cudaError_t e;
+    mark(c, 2);
+    if (c->plan.alg == MESH_ALG_MC) e = launch_emit_mc(c->plan, c->Q64, c->P64, c->stream);
+    else e = launch_emit_halo(c->plan, c->Q64, c->A64, c->P64, c->stream);
+    mark(c, 2);
+    if (e != cudaSuccess) return cuda_fail(c, e, "emit launch");
+    return MESH_OK;
+}
+
+bool degenerate(int64_t nx, int64_t ny, int64_t nz) { return nx < 2 || ny < 2 || nz < 2; }
+
+}  // namespace
+
+extern "C" {
+
+void mesh_params_default(mesh_params *p) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->alg = MESH_ALG_MC;
+    p->iso_type = MESH_DT_F64;
+    p->iso = 0.0;
+    p->eps_type = MESH_DT_F64;
+    p->eps = 1e-3;
+    p->range_type = MESH_DT_I64;
+    p->range[0] = p->range[2] = p->range[4] = -1.0;
+    p->range[1] = p->range[3] = p->range[5] = 1.0;
+}
+
+const char *mesh_status_string(int s) {
+    switch (s) {
+    case MESH_OK: return "ok";
+    case MESH_EINVAL: return "invalid argument";
+    case MESH_ENOMEM: return "out of memory";
+    case MESH_ECUDA: return "CUDA error";
+    case MESH_EDEVICE: return "device-side error";
+    case MESH_ESTATE: return "mesh_fill called without a successful mesh_count";
+    case MESH_ECAPACITY: return "output capacity too small";
+    case MESH_ETOOLARGE: return "volume too large";
+    default: return "unknown status";
+    }
+}
+
+const char *mesh_ctx_last_error(const mesh_ctx *c) { return c ? c->msg.c_str() : ""; }
+
+int mesh_ctx_create(int device, mesh_ctx **out) {
+    if (!out) return MESH_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return e != cudaSuccess ? MESH_ECUDA : MESH_EINVAL;
+    }
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return MESH_ECUDA;
+    mesh_ctx *c = new (std::nothrow) mesh_ctx();
+    if (!c) return MESH_ENOMEM;
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess ||
+        c->misc.ensure(64) != cudaSuccess ||
+        cudaHostAlloc((void **)&c->h_misc, 4 * sizeof(int64_t), cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        mesh_ctx_destroy(c);
+        return MESH_ENOMEM;
+    }
+    c->stream = c->own;
+    *out = c;
+    return MESH_OK;
+}
+
+void mesh_ctx_destroy(mesh_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->vol, &c->tabs, &c->cnt, &c->base, &c->flags, &c->scan, &c->misc, &c->out_v, &c->out_f};
+    for (DevBuf *b : bufs) b->release();
+    for (auto &v : c->ev_pairs)
+        for (cudaEvent_t e : v) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ev_free) cudaEventDestroy(e);
+    if (c->h_misc) cudaFreeHost(c->h_misc);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+}
+
+int mesh_ctx_set_stream(mesh_ctx *c, void *stream) {
+    if (!c) return MESH_EINVAL;
+    c->stream = stream ? (cudaStream_t)stream : c->own;
+    return MESH_OK;
+}
+
+int mesh_output_float_bits(int T, const mesh_params *p, int *bits) {
+    if (!p || !bits) return MESH_EINVAL;
+    int rc = validate(nullptr, T, 0, 0, 0, p);
+    if (rc) return rc;
+    const int tys[4] = {p->range_type, T, p->iso_type, p->eps_type};
+    *bits = out_is_f64(tys, p->alg == MESH_ALG_MT ? 4 : 3) ? 64 : 32;
+    return MESH_OK;
+}
+
+int mesh_count(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
+               const mesh_params *p, int64_t *nverts, int64_t *nfaces) {
+    if (!c || !nverts || !nfaces) return fail(c, MESH_EINVAL, "NULL argument");
+    c->have_plan = 0;
+    c->msg.clear();
+    int rc = validate(c, T, nx, ny, nz, p);
+    if (rc) return rc;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, MESH_ECUDA, "cudaSetDevice");
+    if (degenerate(nx, ny, nz)) {
+        c->nverts = c->nfaces = 0;
+        c->plan = Plan{};
+        c->plan.alg = p->alg;
+        c->have_plan = 2;  // empty mesh
+        *nverts = *nfaces = 0;
+        return MESH_OK;
+    }
+    if (!vol) return fail(c, MESH_EINVAL, "volume is NULL");
+    if ((rc = prepare(c, vol, T, nx, ny, nz, vol_on_device, p))) return rc;
+    if ((rc = run_count(c))) return rc;
+    if ((rc = fetch_misc(c))) return rc;
+    if ((rc = check_err(c))) return rc;
+    c->nverts = c->h_misc[0];
+    c->nfaces = c->h_misc[1];
+    *nverts = c->nverts;
+    *nfaces = c->nfaces;
+    c->have_plan = 1;
+    return MESH_OK;
+}
+
+int mesh_fill(mesh_ctx *c, void *verts, int64_t *faces, int out_on_device) {
+    if (!c) return MESH_EINVAL;
+    if (!c->have_plan) return fail(c, MESH_ESTATE, "mesh_fill without mesh_count");
+    if (c->have_plan == 2 || (c->nverts == 0 && c->nfaces == 0)) return MESH_OK;
+    if ((c->nverts && !verts) || (c->nfaces && !faces)) return fail(c, MESH_EINVAL, "NULL output");
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, MESH_ECUDA, "cudaSetDevice");
+    Plan &P = c->plan;
+    const size_t vb = (size_t)c->nverts * 3 * (P.out64 ? 8 : 4), fbytes = (size_t)c->nfaces * 3 * 8;
+    cudaError_t e;
+    if (out_on_device) {
+        P.verts = verts;
+        P.faces = faces;
+    } else {
+        if ((e = c->out_v.ensure(vb + 16)) != cudaSuccess) return cuda_fail(c, e, "vertex staging");
+        if ((e = c->out_f.ensure(fbytes + 16)) != cudaSuccess) return cuda_fail(c, e, "face staging");
+        P.verts = c->out_v.ptr;
+        P.faces = (int64_t *)c->out_f.ptr;
+    }
+    P.verts_cap = c->nverts;
+    P.faces_cap = c->nfaces;
+    int rc;
+    if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
+    if ((rc = launch_emit(c))) return rc;
+    if (!out_on_device) {
+        if (vb && (e = cudaMemcpyAsync(verts, P.verts, vb, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+            return cuda_fail(c, e, "vertex download");
+        if (fbytes && (e = cudaMemcpyAsync(faces, P.faces, fbytes, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+            return cuda_fail(c, e, "face download");
+    }
+    if ((rc = fetch_misc(c))) return rc;
+    c->have_plan = 0;  // a plan may reference a caller's device volume: one fill per count
+    return check_err(c);
+}
+
+int mesh_extract_device(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz,
+                        const mesh_params *p, void *verts, int64_t verts_cap, int64_t *faces, int64_t faces_cap,
+                        int64_t *counts) {
+    if (!c || !counts) return fail(c, MESH_EINVAL, "NULL argument");
+    c->msg.clear();
+    int rc = validate(c, T, nx, ny, nz, p);
+    if (rc) return rc;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, MESH_ECUDA, "cudaSetDevice");
+    cudaError_t e;
+    if (degenerate(nx, ny, nz)) {
+        if ((e = cudaMemsetAsync(counts, 0, 2 * sizeof(int64_t), c->stream)) != cudaSuccess)
+            return cuda_fail(c, e, "memset");
+        return MESH_OK;
+    }
+    if (!vol) return fail(c, MESH_EINVAL, "volume is NULL");
+    if ((rc = prepare(c, vol, T, nx, ny, nz, 1, p))) return rc;
+    Plan &P = c->plan;
+    P.verts = verts;
+    P.faces = faces;
+    P.verts_cap = verts ? verts_cap : 0;
+    P.faces_cap = faces ? faces_cap : 0;
+    if ((rc = run_count(c))) return rc;
+    if ((rc = launch_emit(c))) return rc;
+    if ((e = cudaMemcpyAsync(counts, P.totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream)) !=
+        cudaSuccess)
+        return cuda_fail(c, e, "count copy");
+    c->have_plan = 0;
+    return MESH_OK;
+}
+
+int mesh_ctx_sync(mesh_ctx *c) {
+    if (!c) return MESH_EINVAL;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, MESH_ECUDA, "cudaSetDevice");
+    int rc = fetch_misc(c);
+    if (rc) return rc;
+    return check_err(c);
+}
+
+int mesh_ctx_enable_timing(mesh_ctx *c, int enable) {
+    if (!c) return MESH_EINVAL;
+    c->timing = enable ? 1 : 0;
+    return MESH_OK;
+}
+
+int mesh_ctx_stage_times(mesh_ctx *c, double *ms, int64_t *launches) {
+    if (!c || !ms || !launches) return MESH_EINVAL;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, MESH_ECUDA, "cudaSetDevice");
+    int rc = MESH_OK;
+    for (int s = 0; s < 3; s++) {
+        ms[s] = 0;
+        launches[s] = 0;
+        auto &v = c->ev_pairs[s];
+        for (size_t i = 0; i + 1 < v.size(); i += 2) {
+            float t = 0;
+            cudaError_t e = cudaEventSynchronize(v[i + 1]);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, v[i], v[i + 1]);
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "stage timing");
+            ms[s] += t;
+            launches[s]++;
+        }
+        for (cudaEvent_t e : v) c->ev_free.push_back(e);
+        v.clear();
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// Internal definitions shared by the host runtime (mesh_api.cu) and the
+// kernels (k_*.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/meshing_gb300.h"
+
+namespace mesh {
+
+// Tiling.  A warp tile covers 32 consecutive x samples (one per lane) and
+// WY+1 consecutive y sample rows, and walks z.  Lane 31 only supplies the
+// x+1 sample of lane 30, so a tile holds 31 cells in x (30 for the emit
+// kernels that also need the -x neighbour cell, kept in lane 0).
+constexpr int WY = 4;            // cell rows per warp tile
+constexpr int WARPS = 8;         // warps per CTA
+constexpr int TILE_X = 31;       // cells per tile in x (classify, MC emit)
+constexpr int TILE_XH = 30;      // cells per tile in x (MT / NSN emit, with -x halo)
+constexpr int ZC = 8;            // cells per activity chunk in z
+
+// Error bits of the device error word.
+constexpr unsigned ERR_SCAN_TIMEOUT = 1u;
+constexpr unsigned ERR_CAPACITY = 2u;
+constexpr unsigned ERR_BOUNDS = 4u;
+
+struct Plan {
+    // volume (Julia layout: x fastest)
+    const void *vol;
+    int64_t nx, ny, nz;
+    int32_t cx, cy, cz;  // cells = samples - 1
+    int32_t T, alg;
+    int32_t out64;       // output eltype is Float64
+    // classification thresholds: v < iso  <=>  v < thr (exact, in the data type)
+    float thr_f;
+    double thr_d;
+    int32_t thr_i;
+    // iso as it enters (iso - v1)/(v2 - v1)
+    float isoq_f;
+    double isoq_d;
+    // MT clamp bounds eps and one(T)-eps, in the clamp type
+    float eps_f, hi_f;
+    double eps_d, hi_d;
+    uint32_t own[8];     // MT: edges owned by a cell, by (x==0)|(y==0)<<1|(z==0)<<2
+    // LinRange node coordinates: exact values (L may be Float32) stored as double,
+    // the same rounded to float, and the node spacings L(p[i+1]-p[i]).
+    const double *xp, *yp, *zp;
+    const double *dx, *dy, *dz;
+    const float *xpf, *ypf, *zpf;
+    const float *dxf, *dyf, *dzf;
+    // z segments and activity chunks
+    int32_t zs, nseg, chunks_per_seg, nchunks;
+    int32_t tiles_x, tiles_y;  // classify tiling (TILE_X x WY cells)
+    // scratch
+    uint32_t *cnt;        // [2][nseg][cy][cx] per-piece vertex / face counts
+    int64_t *base;        // [2][nseg][cy][cx] exclusive prefix in traversal order
+    uint8_t *flags;       // [nchunks][tiles_x][cy] 1 if the tile row has an active cell
+    unsigned long long *scan_state;  // [2][scan tiles] decoupled look-back words
+    unsigned int *scan_ticket;
+    int64_t *totals;      // [2] total vertices, faces
+    unsigned int *err;    // device error word
+    // outputs
+    void *verts;
+    int64_t *faces;
+    int64_t verts_cap, faces_cap;
+    int32_t scan_spin_limit;
+};
+
+inline __host__ __device__ int64_t npieces(const Plan &p) { return (int64_t)p.nseg * p.cy * p.cx; }
+inline __host__ __device__ int64_t piece(const Plan &p, int seg, int y, int x) {
+    return ((int64_t)seg * p.cy + y) * p.cx + x;
+}
+
+// Launchers (each returns cudaError_t of the launch).
+cudaError_t launch_classify(const Plan &p, cudaStream_t s);
+cudaError_t launch_scan(const Plan &p, cudaStream_t s);
+cudaError_t launch_emit(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
+
+}  // namespace mesh
+
+#ifdef __CUDACC__
+namespace mesh {
+
+// Round-to-nearest arithmetic that the compiler may not contract into FMA,
+// matching Julia's separately rounded `+ - * /`.
+template <class F> struct Ar;
+template <> struct Ar<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
+template <> struct Ar<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
+
+// v < iso, exact, in the data type.
+__device__ __forceinline__ bool below(float v, const Plan &p) { return v < p.thr_f; }
+__device__ __forceinline__ bool below(double v, const Plan &p) { return v < p.thr_d; }
+__device__ __forceinline__ bool below(uint16_t v, const Plan &p) { return (int32_t)v < p.thr_i; }
+
+// v2 - v1 in the data type (UInt16 wraps), then converted to Q.
+template <class Q> __device__ __forceinline__ Q tdiff(float v2, float v1) { return (Q)__fsub_rn(v2, v1); }
+template <class Q> __device__ __forceinline__ Q tdiff(double v2, double v1) { return (Q)__dsub_rn(v2, v1); }
+template <class Q> __device__ __forceinline__ Q tdiff(uint16_t v2, uint16_t v1) { return (Q)(uint16_t)(v2 - v1); }
+
+template <class Q> __device__ __forceinline__ Q isoq(const Plan &p);
+template <> __device__ __forceinline__ float isoq<float>(const Plan &p) { return p.isoq_f; }
+template <> __device__ __forceinline__ double isoq<double>(const Plan &p) { return p.isoq_d; }
+
+// (iso - v1) / (v2 - v1) in Julia's promoted types.
+template <class Q, class T> __device__ __forceinline__ Q quotient(T v1, T v2, const Plan &p) {
+    Q den = tdiff<Q>(v2, v1);
+    Q num = Ar<Q>::sub(isoq<Q>(p), (Q)v1);
+    return Ar<Q>::div(num, den);
+}
+
+// Base.max / Base.min on IEEE floats: NaN propagates, -0.0 < +0.0.
+template <class A> __device__ __forceinline__ A jl_max(A x, A y) {
+    A d = Ar<A>::sub(x, y);
+    if (isnan(x) || isnan(y)) return d;
+    return signbit(d) ? y : x;
+}
+template <class A> __device__ __forceinline__ A jl_min(A x, A y) {
+    A d = Ar<A>::sub(x, y);
+    if (isnan(x) || isnan(y)) return d;
+    return signbit(d) ? x : y;
+}
+
+template <class T> __device__ __forceinline__ T ldv(const T *p) { return __ldg(p); }
+template <> __device__ __forceinline__ uint16_t ldv<uint16_t>(const uint16_t *p) {
+    return __ldg(reinterpret_cast<const unsigned short *>(p));
+}
+
+}  // namespace mesh
+#endif

@@ -1,0 +1,218 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Contract (reference semantics): cube cases, face connectivity and vertex/face
+counts bit-exact; positions within 1e-12 (Float64 output) or 2 ulp (Float32
+output) of the oracle.  The kernels reproduce Julia's arithmetic operation by
+operation, so every comparison below is also checked for bit equality.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALGS = {'mc': 'MarchingCubes', 'mt': 'MarchingTetrahedra', 'nsn': 'NaiveSurfaceNets'}
+
+
+def method(pkg, alg, iso=0.0, eps=1e-3):
+    if alg == 'mt':
+        return pkg.MarchingTetrahedra(iso=iso, eps=eps)
+    return getattr(pkg, ALGS[alg])(iso=iso)
+
+
+def assert_same(got, want, what=''):
+    gv, gf = got
+    wv, wf = want
+    assert gv.dtype == wv.dtype, (what, gv.dtype, wv.dtype)
+    assert gv.shape == wv.shape and gf.shape == wf.shape, (what, gv.shape, wv.shape, gf.shape, wf.shape)
+    assert np.array_equal(gf, wf), what
+    if len(gv):
+        fin = np.isfinite(wv)
+        assert np.array_equal(np.isnan(gv), np.isnan(wv)), what
+        err = np.abs(gv[fin].astype(np.float64) - wv[fin].astype(np.float64))
+        if gv.dtype == np.float64:
+            assert err.max(initial=0) <= 1e-12, (what, err.max())
+        else:
+            ulp = np.spacing(np.abs(wv[fin]).astype(np.float32)).astype(np.float64)
+            assert (err <= 2 * ulp).all(), (what, (err / ulp).max())
+        assert np.array_equal(gv, wv, equal_nan=True), (what, 'not bit-exact', err.max())
+
+
+def check(pkg, oracle, A, alg, iso=0.0, eps=1e-3, ranges=((-1, 1),) * 3, device=False):
+    A = np.asfortranarray(A)
+    m = method(pkg, alg, iso, eps)
+    want = oracle.isosurface(A, alg, iso, eps, ranges)
+    if device:
+        import torch
+        t = torch.from_numpy(np.ascontiguousarray(A.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+        v, f = pkg.isosurface(t, m, *ranges)
+        torch.cuda.synchronize()
+        got = (v.cpu().numpy(), f.cpu().numpy())
+    else:
+        got = pkg.isosurface(A, m, *ranges)
+    assert_same(got, want, '%s %s iso=%r eps=%r ranges=%r shape=%s' % (alg, A.dtype, iso, eps, ranges, A.shape))
+    return got
+
+
+def sphere(n, r=0.4, dtype=np.float64, c=(0, 0, 0), shape=None):
+    shape = shape or (n, n, n)
+    g = [np.linspace(-1, 1, s) for s in shape]
+    X, Y, Z = np.meshgrid(*g, indexing='ij')
+    return np.asfortranarray((np.sqrt((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) - r).astype(dtype))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_sphere64_f64(pkg, oracle, cuda, alg):
+    # the 64^3 Float64 sphere fixture (signed distance, r = 0.4, iso 0)
+    v, f = check(pkg, oracle, sphere(64), alg)
+    if alg == 'mc':
+        assert (len(v), len(f)) == (12000, 5996)
+    if alg == 'mt':
+        assert (len(v), len(f)) == (8978, 17952)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_device_and_host_paths_agree(pkg, oracle, cuda, alg):
+    A = sphere(40, 0.55, np.float32)
+    check(pkg, oracle, A, alg, iso=np.float32(0.01), device=True)
+    check(pkg, oracle, A, alg, iso=np.float32(0.01), device=False)
+
+
+TYPE_CASES = [
+    (np.float64, 0.0, 1e-3, (-1, 1)),
+    (np.float64, np.float32(0.25), np.float32(1e-3), (0.0, 2.5)),
+    (np.float32, 0.0, 1e-3, (-1, 1)),
+    (np.float32, np.float32(0.1), np.float32(1e-3), (-1, 1)),
+    (np.float32, np.float32(0.1), 1e-3, (np.float32(-2), np.float32(3))),
+    (np.float32, 0, 1e-4, (0, 1)),
+    (np.float32, np.float32(-0.3), np.float32(1e-2), (0.0, 1.0)),
+    (np.uint16, 500, 1e-3, (-1, 1)),
+    (np.uint16, 500, np.float32(1e-3), (np.float32(0), np.float32(7))),
+    (np.uint16, np.float32(300.5), np.float32(1e-3), (-1, 1)),
+    (np.uint16, 250.25, 1e-3, (0.0, 1.0)),
+]
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+@pytest.mark.parametrize('case', range(len(TYPE_CASES)))
+def test_random_grids_all_types(pkg, oracle, cuda, alg, case):
+    dt, iso, eps, r = TYPE_CASES[case]
+    rng = np.random.default_rng(100 + case)
+    for trial in range(4):
+        shape = tuple(int(s) for s in rng.integers(2, 18, 3))
+        if dt == np.uint16:
+            A = rng.integers(0, 1000, shape).astype(np.uint16)
+        else:
+            A = rng.standard_normal(shape).astype(dt)
+        check(pkg, oracle, A, alg, iso, eps, (r, r, r))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_ragged_multi_tile_shapes(pkg, oracle, cuda, alg):
+    # shapes spanning several x tiles (31/30 cells), y tiles (4 rows), z segments and chunks
+    rng = np.random.default_rng(7)
+    for shape in [(67, 45, 133), (33, 9, 70), (95, 13, 17), (2, 70, 41), (70, 2, 9), (31, 5, 200)]:
+        A = sphere(0, 0.7, np.float32, c=(0.1, -0.2, 0.05), shape=shape)
+        A += np.float32(0.05) * rng.standard_normal(shape).astype(np.float32)
+        check(pkg, oracle, A, alg, np.float32(0))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_sparse_surface_chunk_skipping(pkg, oracle, cuda, alg):
+    # a small object: most z chunks and tiles are empty and skipped
+    for c in [(0.8, 0.8, 0.8), (-0.85, 0.1, -0.9), (0.0, -0.9, 0.3)]:
+        A = sphere(0, 0.12, np.float64, c=c, shape=(150, 90, 200))
+        check(pkg, oracle, A, alg)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_all_256_cases(pkg, oracle, cuda, alg):
+    # every cube case as a single cell, plus all of them planted in one grid
+    for c in range(256):
+        A = np.ones((2, 2, 2), np.float32)
+        order = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+        for k, (x, y, z) in enumerate(order):
+            if (c >> k) & 1:
+                A[x, y, z] = -1 - 0.37 * k
+            else:
+                A[x, y, z] = 0.5 + 0.21 * k
+        check(pkg, oracle, A, alg, np.float32(0))
+    A = np.ones((32, 32, 2), np.float32)
+    rng = np.random.default_rng(3)
+    for c in range(256):
+        i, j = divmod(c, 16)
+        for k, (x, y, z) in enumerate([(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1),
+                                       (0, 1, 1)]):
+            A[2 * i + x, 2 * j + y, z] = -rng.random() if (c >> k) & 1 else rng.random()
+    check(pkg, oracle, A, alg, np.float32(0))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_nan_inf_ties_and_signed_zero(pkg, oracle, cuda, alg):
+    rng = np.random.default_rng(11)
+    for dt in (np.float32, np.float64):
+        A = rng.standard_normal((12, 11, 13)).astype(dt)
+        A.flat[rng.choice(A.size, 40, replace=False)] = np.nan
+        A.flat[rng.choice(A.size, 20, replace=False)] = np.inf
+        A.flat[rng.choice(A.size, 20, replace=False)] = -np.inf
+        A.flat[rng.choice(A.size, 60, replace=False)] = 0.0  # ties with iso
+        A.flat[rng.choice(A.size, 30, replace=False)] = -0.0
+        check(pkg, oracle, A, alg, dt(0) if dt == np.float32 else 0.0)
+        # ranges through zero at a node (-0.0 handling of still coordinates)
+        check(pkg, oracle, A, alg, 0.0, 1e-3, ((-1.0, 1.0), (0.0, 2.0), (-3.0, 0.0)))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_uint16_wraparound(pkg, oracle, cuda, alg):
+    rng = np.random.default_rng(5)
+    A = np.where(rng.random((20, 21, 22)) < 0.5, rng.integers(0, 400, (20, 21, 22)),
+                 rng.integers(600, 65535, (20, 21, 22))).astype(np.uint16)
+    check(pkg, oracle, A, alg, 500)
+    check(pkg, oracle, A, alg, np.float32(500.5), np.float32(1e-3))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_degenerate_volumes(pkg, oracle, cuda, alg):
+    for shape in [(1, 5, 5), (5, 1, 5), (5, 5, 1), (0, 4, 4), (2, 2, 2)]:
+        A = np.random.default_rng(1).standard_normal(shape)
+        check(pkg, oracle, A, alg)
+    check(pkg, oracle, np.ones((4, 4, 4)), alg)        # no crossings
+    check(pkg, oracle, -np.ones((4, 4, 4)), alg)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_gyroid_256_f32(pkg, oracle, cuda, alg):
+    # Float32 gyroid on [-3pi, 3pi]^3, iso 0 (Float64, the MarchingCubes() default)
+    g = np.linspace(-3 * np.pi, 3 * np.pi, 256).astype(np.float32)
+    X, Y, Z = np.meshgrid(g, g, g, indexing='ij')
+    A = np.asfortranarray(np.sin(X) * np.cos(Y) + np.sin(Y) * np.cos(Z) + np.sin(Z) * np.cos(X))
+    r = (-3 * np.pi, 3 * np.pi)
+    check(pkg, oracle, A, alg, 0.0, 1e-3, (r, r, r))
+    check(pkg, oracle, A, alg, np.float32(0), np.float32(1e-3), ((-3, 3),) * 3)
+
+
+def test_extract_device_capacity(pkg, oracle, cuda):
+    import torch
+    A = sphere(48, 0.5, np.float32)
+    t = torch.from_numpy(np.ascontiguousarray(A.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+    want = oracle.isosurface(A, 'mc', np.float32(0))
+    m = pkg.MarchingCubes(iso=np.float32(0))
+    verts = torch.empty((len(want[0]), 3), dtype=torch.float32, device='cuda')
+    faces = torch.empty((len(want[1]), 3), dtype=torch.int64, device='cuda')
+    counts = pkg.isosurface_device(t, m, verts=verts, faces=faces)
+    pkg.api.sync()
+    assert counts.tolist() == [len(want[0]), len(want[1])]
+    assert_same((verts.cpu().numpy(), faces.cpu().numpy()), want)
+    small = torch.empty((10, 3), dtype=torch.float32, device='cuda')
+    counts = pkg.isosurface_device(t, m, verts=small, faces=faces)
+    with pytest.raises(pkg.MeshError) as ei:
+        pkg.api.sync()
+    assert ei.value.status == 6  # MESH_ECAPACITY
+    assert counts.tolist() == [len(want[0]), len(want[1])]
+
+
+def test_fill_without_count_is_rejected(pkg, cuda):
+    c = pkg.Context(0)
+    rc = pkg.load_library().mesh_fill(c.handle, None, None, 0)
+    assert rc == 5  # MESH_ESTATE

@@ -1,0 +1,152 @@
+"""Pins the CPU oracle to the reference's own known-answer tests (test/runtests.jl)
+and cross-checks its two restatements (C and pure Python)."""
+import numpy as np
+import pytest
+
+import pyoracle
+
+
+def test_get_cubeindex_kats(oracle):
+    # test/runtests.jl:15-27
+    assert oracle.cubeindex([0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8], 0.35) == 0x07
+    assert oracle.cubeindex([0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2], 0.75) == 0x07
+    assert oracle.cubeindex([0.9, 0.8, 0.7, 0.6, 0.5, 0.4, 0.3, 0.2], 0.5) == 0xe0
+
+
+def test_vertex_interp_kats(oracle):
+    # test/runtests.jl:29-33
+    assert oracle.vertex_interp(0, (0, 0, 0), (0, 1, 0), -1, 1) == (0, 0.5, 0)
+    assert oracle.vertex_interp(-1, (0, 0, 0), (0, 1, 0), -1, 1) == (0, 0, 0)
+    assert oracle.vertex_interp(1, (0, 0, 0), (0, 1, 0), -1, 1) == (0, 1, 0)
+
+
+def _norm_sdf(lo, hi, step):
+    n = int(round((hi - lo) / step)) + 1
+    g = lo + step * np.arange(n)
+    X, Y, Z = np.meshgrid(g, g, g, indexing='ij')
+    return np.asfortranarray(np.sqrt(X * X + Y * Y + Z * Z))
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt'])
+def test_respect_origin(oracle, alg):
+    # test/runtests.jl:127-149: norm_sdf on -1:0.01:1, iso 0.5, default X/Y/Z
+    A = _norm_sdf(-1.0, 1.0, 0.01)
+    v, f = oracle.isosurface(A, alg, iso=0.5)
+    assert np.allclose(v.mean(axis=0), 0, atol=0.015)
+    for i in range(3):
+        assert abs(v[:, i].max() - 0.5) <= 0.001
+        assert abs(v[:, i].min() + 0.5) <= 0.001
+    assert f.min() >= 1 and f.max() <= len(v)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt'])
+def test_forward_diff_value(oracle, alg):
+    # value part of test/runtests.jl:98-125: mean vertex radius equals iso
+    rng = (-2.0, 2.0)
+    A = _norm_sdf(-2.0, 2.0, 0.01)
+    v, _ = oracle.isosurface(A, alg, iso=0.85, ranges=(rng, rng, rng))
+    assert abs(np.linalg.norm(v, axis=1).mean() - 0.85) <= 1e-2
+
+
+def test_defaults(oracle):
+    # test/runtests.jl:76-79: isosurface(A) == isosurface(A, MarchingCubes())
+    A = np.random.default_rng(1).random((10, 10, 10))
+    a = oracle.isosurface(A)
+    b = oracle.isosurface(A, 'mc', iso=0.0)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_mixed_types(oracle):
+    # test/runtests.jl:81-97: MT on Float64 vs Float32 copies of the same field
+    s = np.random.default_rng(9).standard_normal((10, 10, 10))
+    r = ((0, 1), (0, 1), (0, 1))
+    v1, f1 = oracle.isosurface(s, 'mt', ranges=r)
+    v2, f2 = oracle.isosurface(s.astype(np.float32), 'mt', ranges=r)
+    assert len(v1) == len(v2) and np.array_equal(f1, f2)
+
+
+@pytest.mark.parametrize('dtype,iso,eps,rt,alg,bits', [
+    (np.float64, 0.2, 1e-4, 4, 'mt', 64),
+    (np.float32, np.float32(0.2), np.float32(1e-4), 4, 'mt', 32),
+    (np.float64, np.float32(0.2), np.float32(1e-4), 4, 'mt', 64),
+    (np.float32, 0.0, 1e-3, 4, 'mc', 64),
+    (np.float32, np.float32(0), 1e-3, 4, 'mc', 32),
+    (np.float32, 0, 1e-3, 4, 'mc', 32),
+    (np.float32, np.float32(0), 1e-3, 3, 'mc', 64),
+    (np.uint16, 500, 1e-3, 4, 'mc', 64),
+    (np.uint16, np.float32(500), 1e-3, 4, 'mc', 32),
+    (np.uint16, 500, 1e-3, 2, 'mc', 32),
+    (np.float32, np.float32(0), 1e-3, 4, 'mt', 64),
+])
+def test_output_eltype_rule(oracle, dtype, iso, eps, rt, alg, bits):
+    # test/runtests.jl:35-75: float(promote_type(range, data, iso[, eps]))
+    assert oracle.output_bits(dtype, alg, iso, eps, rt) == bits
+
+
+def _sphere(n, r=0.4):
+    g = np.linspace(-1, 1, n)
+    X, Y, Z = np.meshgrid(g, g, g, indexing='ij')
+    return np.asfortranarray(np.sqrt(X * X + Y * Y + Z * Z) - r)
+
+
+def test_sphere64_counts(oracle):
+    # 64^3 Float64 sphere fixture: counts restated from the reference's counting rules
+    A = _sphere(64)
+    v, f = oracle.isosurface(A, 'mc')
+    assert (len(v), len(f)) == (12000, 5996)
+    v, f = oracle.isosurface(A, 'mt')
+    assert (len(v), len(f)) == (8978, 17952)
+
+
+def _edges(f):
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+    return e
+
+
+@pytest.mark.parametrize('alg', ['mt', 'nsn'])
+def test_closed_manifold_sphere(oracle, alg):
+    # MT (and our NSN) produce watertight, consistently oriented meshes:
+    # every directed edge appears once and its reverse once; Euler characteristic 2.
+    v, f = oracle.isosurface(_sphere(48, 0.55), alg)
+    e = _edges(f)
+    key = e[:, 0] * (len(v) + 1) + e[:, 1]
+    rkey = e[:, 1] * (len(v) + 1) + e[:, 0]
+    assert len(np.unique(key)) == len(key)
+    assert np.array_equal(np.sort(key), np.sort(rkey))
+    assert len(v) - len(key) // 2 + len(f) == 2
+    # outward orientation (increasing values) for NSN: positive signed volume
+    if alg == 'nsn':
+        p = v[f - 1]
+        vol = np.einsum('ij,ij->i', p[:, 0], np.cross(p[:, 1], p[:, 2])).sum() / 6
+        assert vol > 0
+
+
+def test_c_oracle_matches_python_restatement(oracle):
+    rng = np.random.default_rng(0)
+    cases = [(np.float64, 0.0), (np.float32, np.float32(0.1)), (np.float32, 0.0), (np.float32, 0),
+             (np.uint16, 500), (np.uint16, np.float32(300.5)), (np.uint16, 250.25)]
+    for trial in range(6):
+        sh = tuple(int(s) for s in rng.integers(2, 7, 3))
+        for dt, iso in cases:
+            if dt == np.uint16:
+                A = rng.integers(0, 1000, sh).astype(np.uint16)
+            else:
+                A = rng.standard_normal(sh).astype(dt)
+            for alg in ('mc', 'mt'):
+                for eps in ([1e-3, np.float32(1e-3)] if alg == 'mt' else [1e-3]):
+                    for rg in (((-1, 1),) * 3, ((np.float32(-2), np.float32(3)),) * 3, ((0.0, 1.5),) * 3):
+                        a = oracle.isosurface(A, alg, iso, eps, rg)
+                        b = pyoracle.isosurface(A, alg, iso, eps, rg)
+                        assert a[0].dtype == b[0].dtype
+                        assert np.array_equal(a[1], b[1])
+                        assert np.array_equal(a[0], b[0], equal_nan=True)
+
+
+def test_uint16_wraparound_is_reproduced(oracle):
+    # vertex_interp on UInt16 data: v2 - v1 wraps modulo 2^16 (src/marching_cubes.jl:101)
+    A = np.zeros((2, 2, 2), np.uint16)
+    A[0, 0, 0] = 900  # corner 1 above iso 500, the rest below: edge (1 -> 2) has v2 - v1 = 0 - 900 (wraps)
+    v, f = oracle.isosurface(A, 'mc', iso=500)
+    mu = (500 - 900) / float((0 - 900) % 65536)
+    assert len(v) == 3 and len(f) == 1
+    assert np.isclose(v[0, 0], -1 + mu * 2)  # edge 1 runs along +x from x=-1
