@@ -50,8 +50,9 @@ def sines_host(n, z0, nz, seed=SEED):
         ex = np.exp(1j * (2 * np.pi * w[0]) * g).astype(np.complex64)
         ey = np.exp(1j * (2 * np.pi * w[1]) * g).astype(np.complex64)
         ez = np.exp(1j * ((2 * np.pi * w[2]) * g[z0:z0 + nz] + ph)).astype(np.complex64)
+        exy = ey[:, None] * ex[None, :]
         for k in range(nz):
-            out[k] += np.float32(a) * (ez[k] * (ey[:, None] * ex[None, :])).imag
+            out[k] += np.float32(a) * (ez[k] * exy).imag
     return out
 
 
@@ -144,7 +145,7 @@ def cpu_baseline(n, planes, steps=1, warmup=0):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    planes = args.cpu_planes
+    planes = args.cpu_planes or 32
     val, dt, nv, nf, vox = cpu_baseline(args.n, planes, steps=args.steps, warmup=args.warmup)
     sample = ('z slab %dx%dx%d (%.0f M samples) of the benchmark field, CPU restatement of MarchingCubes '
               '(oracle/oracle.c, single-threaded like Meshing.jl), %.2f s per step' %
@@ -263,10 +264,11 @@ def run_ours(args, rank, world, dist):
     pipe_gbs = (in_b + out_b) / (ms * 1e-3) / 1e9
     cpu = None
     if world == 1 and not args.no_cpu:
-        cval, cdt, _, _, cvox = cpu_baseline(n, args.cpu_planes)
+        planes = args.cpu_planes or 128
+        cval, cdt, _, _, cvox = cpu_baseline(n, planes)
         cpu = {'value': cval, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port',
                'sample': 'z slab %dx%dx%d of the same field, CPU restatement of MarchingCubes (oracle/oracle.c, '
-                         'single-threaded like Meshing.jl), %.2f s' % (n, n, args.cpu_planes + 1, cdt)}
+                         'single-threaded like Meshing.jl), %.2f s' % (n, n, planes + 1, cdt)}
     line = {
         'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes',
         'value': vox * world / (ms * 1e-3) / 1e9,
@@ -296,7 +298,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--n', type=int, default=N_DEFAULT, help='grid size per axis (default 1024)')
-    ap.add_argument('--cpu-planes', type=int, default=128, help='z planes of the CPU sample')
+    ap.add_argument('--cpu-planes', type=int, default=None,
+                    help='z cell planes of the CPU sample (default 128; 32 for --impl reference)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     args = ap.parse_args()
     world = int(os.environ.get('WORLD_SIZE', '1'))

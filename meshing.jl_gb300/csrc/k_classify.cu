@@ -72,6 +72,9 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
 #pragma unroll
     for (int r = 0; r < WY; r++) cntv[r] = cntf[r] = act[r] = 0;
 
+    // lanes whose sample exists (x < nx): only their bits take part in the uniform test
+    const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
+    const uint32_t cellm = __ballot_sync(FULL, cellx);
     uint32_t mlo[WY + 1];
 #pragma unroll
     for (int r = 0; r <= WY; r++) {
@@ -81,27 +84,45 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
 
     for (int z = zbeg; z < zend; z += U) {
         T v[U][WY + 1];
+        const int64_t off = sxy * (int64_t)(z + 1);
+        if (z + U <= zend) {
 #pragma unroll
-        for (int u = 0; u < U; u++)
+            for (int u = 0; u < U; u++)
 #pragma unroll
-            for (int r = 0; r <= WY; r++)
-                v[u][r] = (rowok[r] && z + 1 + u <= zend) ? ldv(rowp[r] + sxy * (int64_t)(z + 1 + u)) : T(0);
+                for (int r = 0; r <= WY; r++) v[u][r] = rowok[r] ? ldv(rowp[r] + off + sxy * u) : T(0);
+        } else {
+#pragma unroll
+            for (int u = 0; u < U; u++)
+#pragma unroll
+                for (int r = 0; r <= WY; r++)
+                    v[u][r] = (rowok[r] && z + 1 + u <= zend) ? ldv(rowp[r] + off + sxy * u) : T(0);
+        }
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const int zc = z + u;
             if (zc >= zend) break;  // warp-uniform
             uint32_t mhi[WY + 1];
+            uint32_t all1 = xval, any1 = 0;
 #pragma unroll
-            for (int r = 0; r <= WY; r++) mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
+            for (int r = 0; r <= WY; r++) {
+                mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
+                all1 &= mlo[r] & mhi[r];
+                any1 |= mlo[r] | mhi[r];
+            }
+            // warp-uniform early out: every corner of every cell in this step on one side
+            if (all1 != xval && any1 != 0) {
 #pragma unroll
-            for (int r = 0; r < WY; r++) {
-                const bool ok = cellx && (y0 + r < p.cy);
-                const unsigned a = (mlo[r] >> lane) & 3u, b = (mlo[r + 1] >> lane) & 3u;
-                const unsigned c = (mhi[r] >> lane) & 3u, d = (mhi[r + 1] >> lane) & 3u;
-                const unsigned cm = mc_case(a, b, c, d);
-                const bool active = ok && cm != 0u && cm != 255u;
-                if (active) {
+                for (int r = 0; r < WY; r++) {
+                    // bit l: cell l has corners on both sides (bits l, l+1 of the four masks)
+                    const uint32_t and4 = mlo[r] & mlo[r + 1] & mhi[r] & mhi[r + 1];
+                    const uint32_t or4 = mlo[r] | mlo[r + 1] | mhi[r] | mhi[r + 1];
+                    const uint32_t actm = (or4 | (or4 >> 1)) & ~(and4 & (and4 >> 1)) & cellm;
+                    if (actm == 0u || y0 + r >= p.cy) continue;  // warp-uniform
                     act[r] = 1;
+                    if (!((actm >> lane) & 1u)) continue;
+                    const unsigned a = (mlo[r] >> lane) & 3u, b = (mlo[r + 1] >> lane) & 3u;
+                    const unsigned c = (mhi[r] >> lane) & 3u, d = (mhi[r + 1] >> lane) & 3u;
+                    const unsigned cm = mc_case(a, b, c, d);
                     if (ALG == MESH_ALG_MC) {
                         const uint32_t t = s_tab[cm];
                         cntv[r] += t & 15u;
@@ -131,8 +152,7 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
                 uint8_t mine = 0;
 #pragma unroll
                 for (int r = 0; r < WY; r++) {
-                    const unsigned any = __ballot_sync(FULL, act[r] != 0);
-                    if (lane == r) mine = any != 0;
+                    if (lane == r) mine = act[r] != 0;  // act[] is warp-uniform
                     act[r] = 0;
                 }
                 if (lane < WY && y0 + lane < p.cy)

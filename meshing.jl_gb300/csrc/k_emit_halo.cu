@@ -56,10 +56,6 @@ __device__ __forceinline__ unsigned mt_case(unsigned a, unsigned b, unsigned c, 
            ((d >> 1) << 6) | ((c >> 1) << 7);
 }
 
-template <class T> __device__ __forceinline__ T shfl_down1(T v) { return __shfl_down_sync(FULL, v, 1); }
-template <> __device__ __forceinline__ uint16_t shfl_down1<uint16_t>(uint16_t v) {
-    return (uint16_t)__shfl_down_sync(FULL, (unsigned)v, 1);
-}
 
 // vertPos (src/marching_tetrahedra.jl:42-55) for voxel edge e of cell (x,y,z);
 // corner values in MT corner order.

@@ -73,6 +73,7 @@ struct mesh_ctx {
     std::string msg;
     // stage timing (diagnostics)
     int timing = 0;
+    int force_fp64 = 0;  // MESHING_GB300_FORCE_FP64=1: evaluate every Float64 position in FP64
     std::vector<cudaEvent_t> ev_free;
     std::vector<cudaEvent_t> ev_pairs[3];  // start, stop, start, stop, ...
 };
@@ -243,13 +244,15 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
         P.vol = c->vol.ptr;
     }
 
-    // coordinate tables: xp yp zp dx dy dz (double) then the same as float
+    // coordinate tables: xp yp zp dx dy dz (double), the same as float, then the
+    // hi/lo float split of the nodes and spacings
     const int64_t ntab = nx + ny + nz;
-    const size_t tbytes = (size_t)ntab * 2 * (sizeof(double) + sizeof(float));
+    const size_t tbytes = (size_t)ntab * 2 * (sizeof(double) + sizeof(float)) + (size_t)ntab * 4 * sizeof(float);
     double *h = (double *)malloc(tbytes);
     if (!h) return fail(c, MESH_ENOMEM, "host table buffer");
     double *hp = h, *hd = h + ntab;
     float *hpf = (float *)(h + 2 * ntab), *hdf = hpf + ntab;
+    float *hs = hdf + ntab;  // p_hi, p_lo, d_hi, d_lo
     const int64_t ns[3] = {nx, ny, nz};
     int64_t off = 0;
     for (int a = 0; a < 3; a++) {
@@ -260,9 +263,14 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
                 d = hp[off + i + 1] - hp[off + i];
                 if (L32) d = (double)((float)hp[off + i + 1] - (float)hp[off + i]);
             }
+            const double v = hp[off + i];
             hd[off + i] = d;
-            hpf[off + i] = (float)hp[off + i];
+            hpf[off + i] = (float)v;
             hdf[off + i] = (float)d;
+            hs[off + i] = (float)v;
+            hs[ntab + off + i] = (float)(v - (double)(float)v);
+            hs[2 * ntab + off + i] = (float)d;
+            hs[3 * ntab + off + i] = (float)(d - (double)(float)d);
         }
         off += ns[a];
     }
@@ -277,6 +285,9 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     float *fp = (float *)(dp + 2 * ntab);
     P.xpf = fp; P.ypf = fp + nx; P.zpf = fp + nx + ny;
     P.dxf = fp + ntab; P.dyf = P.dxf + nx; P.dzf = P.dxf + nx + ny;
+    P.split = fp + 2 * ntab;
+    P.ntab = ntab;
+    P.force_fp64 = c->force_fp64;
 
     // scratch
     const int64_t np = npieces(P);
@@ -294,6 +305,7 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + (size_t)st * 2 * sizeof(unsigned long long));
     P.totals = (int64_t *)c->misc.ptr;
     P.err = (unsigned int *)((int64_t *)c->misc.ptr + 2);
+    P.work = (unsigned int *)((int64_t *)c->misc.ptr + 3);
     P.scan_spin_limit = 1 << 24;
     return MESH_OK;
 }
@@ -416,6 +428,8 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
         return MESH_ENOMEM;
     }
     c->stream = c->own;
+    const char *ff = getenv("MESHING_GB300_FORCE_FP64");
+    c->force_fp64 = ff && ff[0] == '1';
     *out = c;
     return MESH_OK;
 }

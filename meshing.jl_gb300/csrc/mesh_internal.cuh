@@ -47,6 +47,12 @@ struct Plan {
     const double *dx, *dy, *dz;
     const float *xpf, *ypf, *zpf;
     const float *dxf, *dyf, *dzf;
+    // float pairs hi + lo of the node coordinates and spacings (for the exact
+    // float fast path of Float64 positions rounded to Float32): split[k][ntab]
+    // with k = 0 p_hi, 1 p_lo, 2 d_hi, 3 d_lo, nodes of x, then y, then z
+    const float *split;
+    int64_t ntab;
+    int32_t force_fp64;   // disable the float fast path (diagnostics)
     // z segments and activity chunks
     int32_t zs, nseg, chunks_per_seg, nchunks;
     int32_t tiles_x, tiles_y;  // classify tiling (TILE_X x WY cells)
@@ -58,6 +64,7 @@ struct Plan {
     unsigned int *scan_ticket;
     int64_t *totals;      // [2] total vertices, faces
     unsigned int *err;    // device error word
+    unsigned int *work;   // work-item counter of the persistent kernels
     // outputs
     void *verts;
     int64_t *faces;
@@ -127,6 +134,40 @@ template <class A> __device__ __forceinline__ A jl_min(A x, A y) {
     A d = Ar<A>::sub(x, y);
     if (isnan(x) || isnan(y)) return d;
     return signbit(d) ? x : y;
+}
+
+// fl32(fl64(p1 + fl64(mu * d))) for a Float32 mu and Float64 p1, d given as
+// float pairs (p1 = p1h + p1l, d = dh + dl up to 2^-48 relative), without FP64
+// instructions.  A float-float estimate r of p1 + mu*d is formed with
+// TwoProduct / TwoSum; together with the two Float64 roundings of the
+// reference it lies within E = 2^-42 (|p1| + |mu d|) of the exact value (the
+// analysis gives about 2^-44).  If no Float32 rounding boundary lies within E
+// of r, the reference result rounds to the same float f = fl32(r) and the
+// function returns true; otherwise (or near underflow/overflow) it returns
+// false and the caller evaluates the Float64 expression.
+__device__ __forceinline__ bool fast_f32_pos(float mu, float p1h, float p1l, float dh, float dl, float &out) {
+    const float ph = __fmul_rn(mu, dh);
+    const float pe = __fmaf_rn(mu, dh, -ph);  // exact: mu*dh == ph + pe
+    const float ql = __fmul_rn(mu, dl);
+    const float sh = __fadd_rn(p1h, ph);      // TwoSum(p1h, ph) = sh + se
+    const float bb = __fsub_rn(sh, p1h);
+    const float se = __fadd_rn(__fsub_rn(p1h, __fsub_rn(sh, bb)), __fsub_rn(ph, bb));
+    const float lo = __fadd_rn(se, __fadd_rn(p1l, __fadd_rn(pe, ql)));
+    const float f = __fadd_rn(sh, lo);
+    const float t = __fadd_rn(__fsub_rn(sh, f), lo);  // r - f
+    const unsigned fb = __float_as_uint(f) & 0x7fffffffu;
+    const int e = (int)(fb >> 23);
+    out = f;
+    if (e < 64 || e > 190) return false;
+    float hu = __uint_as_float((unsigned)(e - 24) << 23);  // half ulp of |f|
+    if ((fb & 0x7fffffu) == 0u) hu = __fmul_rn(hu, 0.5f);  // power of two: the gap towards zero is half
+    const float E = __fmul_rn(__fadd_rn(fabsf(p1h), fabsf(ph)), 0x1p-42f);
+    return __fadd_rn(__fmul_rn(fabsf(t), 1.0000002f), E) < hu;
+}
+
+template <class T> __device__ __forceinline__ T shfl_down1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+template <> __device__ __forceinline__ uint16_t shfl_down1<uint16_t>(uint16_t v) {
+    return (uint16_t)__shfl_down_sync(0xffffffffu, (unsigned)v, 1);
 }
 
 template <class T> __device__ __forceinline__ T ldv(const T *p) { return __ldg(p); }

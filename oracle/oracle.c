@@ -175,16 +175,23 @@ static int push_face(orc_mesh *m, int64_t a, int64_t b, int64_t cc) {
 
 static const int MC_CORNER[8][3] = {{0,0,0},{1,0,0},{1,1,0},{0,1,0},{0,0,1},{1,0,1},{1,1,1},{0,1,1}};
 
-static int mc_cell(const orc_ctx *c, int64_t xi, int64_t yi, int64_t zi, double v[8], double p[8][3]) {
+/* iso_vals and _get_cubeindex (src/marching_cubes.jl:42-53) */
+static int mc_case(const orc_ctx *c, int64_t xi, int64_t yi, int64_t zi, double v[8]) {
     int ci = 0;
     for (int k = 0; k < 8; k++) {
         v[k] = load(c, xi + MC_CORNER[k][0], yi + MC_CORNER[k][1], zi + MC_CORNER[k][2]);
         if (below(c, v[k])) ci |= 1 << k;
+    }
+    return ci;
+}
+
+/* mc_vert_points (src/marching_cubes.jl:111-120), only for cells with triangles */
+static void mc_points(const orc_ctx *c, int64_t xi, int64_t yi, int64_t zi, double p[8][3]) {
+    for (int k = 0; k < 8; k++) {
         p[k][0] = c->xp[xi + MC_CORNER[k][0]];
         p[k][1] = c->yp[yi + MC_CORNER[k][1]];
         p[k][2] = c->zp[zi + MC_CORNER[k][2]];
     }
-    return ci;
 }
 
 static void vertex_interp(const orc_ctx *c, const double p1[3], const double p2[3], double v1, double v2, double out[3]) {
@@ -197,8 +204,9 @@ static int run_mc(const orc_ctx *c, orc_mesh *m) {
     for (int64_t xi = 0; xi + 1 < c->nx; xi++)
         for (int64_t yi = 0; yi + 1 < c->ny; yi++)
             for (int64_t zi = 0; zi + 1 < c->nz; zi++) {
-                int ci = mc_cell(c, xi, yi, zi, v, p);
+                int ci = mc_case(c, xi, yi, zi, v);
                 if (ci == 0 || ci == 255) continue;
+                mc_points(c, xi, yi, zi, p);
                 int64_t fct = m->nverts;
                 const uint8_t *row = R_MC_VERTS[ci - 1];
                 for (int i = 0; i < 12; i++) {
@@ -361,8 +369,9 @@ static int run_nsn(const orc_ctx *c, orc_mesh *m) {
     for (int64_t xi = 0; xi < cx; xi++)
         for (int64_t yi = 0; yi < cy; yi++)
             for (int64_t zi = 0; zi < cz; zi++) {
-                int ci = mc_cell(c, xi, yi, zi, v, p);
+                int ci = mc_case(c, xi, yi, zi, v);
                 if (ci == 0 || ci == 255) continue;
+                mc_points(c, xi, yi, zi, p);
                 double s[3] = {0, 0, 0};
                 int n = 0;
                 for (int e = 0; e < 12; e++) {
