@@ -54,7 +54,7 @@ typedef enum {
     MESH_EDEVICE = 4,      /* a kernel reported an error (bounded wait expired, bounds check) */
     MESH_ESTATE = 5,       /* mesh_fill without a preceding successful mesh_count */
     MESH_ECAPACITY = 6,    /* output buffers smaller than the mesh */
-    MESH_ETOOLARGE = 7     /* volume beyond the engine's index limits */
+    MESH_ETOOLARGE = 7     /* volume beyond the engine's index limits (more than 2^21 samples on an axis) */
 } mesh_status;
 
 /* Mirrors MarchingCubes{T}(iso) / MarchingTetrahedra{T,E}(iso, eps) plus the

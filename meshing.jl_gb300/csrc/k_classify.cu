@@ -8,8 +8,8 @@
 // the strict `v < iso` tests of a whole row into a bit mask, from which every
 // lane assembles its 8-corner case without further memory traffic.
 //
-// Outputs: cnt[v|f][seg][y][x] (u32) -- vertices first-created / faces emitted
-// by column x,y inside z segment seg -- and one activity byte per
+// Outputs: cnt[v|f|a][seg][y][x] (u32) -- vertices first-created, faces emitted
+// and active cells of column x,y inside z segment seg -- and one activity byte per
 // (z chunk, x tile, y row) that lets the emit kernels skip empty chunks.
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
@@ -68,9 +68,9 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
         rowp[r] = rowok[r] ? vol + xs + p.nx * (int64_t)(y0 + r) : vol;
     }
 
-    uint32_t cntv[WY], cntf[WY], act[WY];
+    uint32_t cntv[WY], cntf[WY], cnta[WY], act[WY];
 #pragma unroll
-    for (int r = 0; r < WY; r++) cntv[r] = cntf[r] = act[r] = 0;
+    for (int r = 0; r < WY; r++) cntv[r] = cntf[r] = cnta[r] = act[r] = 0;
 
     // lanes whose sample exists (x < nx): only their bits take part in the uniform test
     const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
                     if (actm == 0u || y0 + r >= p.cy) continue;  // warp-uniform
                     act[r] = 1;
                     if (!((actm >> lane) & 1u)) continue;
+                    cnta[r] += 1;
                     const unsigned a = (mlo[r] >> lane) & 3u, b = (mlo[r + 1] >> lane) & 3u;
                     const unsigned c = (mhi[r] >> lane) & 3u, d = (mhi[r + 1] >> lane) & 3u;
                     const unsigned cm = mc_case(a, b, c, d);
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
                 const int64_t i = piece(p, seg, y0 + r, xs);
                 p.cnt[i] = cntv[r];
                 p.cnt[np + i] = cntf[r];
+                p.cnt[2 * np + i] = cnta[r];
             }
         }
     }

@@ -1,28 +1,30 @@
 // K3 (Marching Cubes) -- emit vertices and faces at the scanned offsets.
 //
 // Replaces process_mc_voxel! (src/marching_cubes.jl:67-92), vertex_interp
-// (:100-104) and mc_vert_points (:111-120).
+// (:100-104) and mc_vert_points (:111-120).  Two kernels:
 //
-// Walk.  The warp tiling is the classify kernel's (31 x-cells by WY y-cells,
-// one z segment).  Every lane walks its column in z with a running (vertex,
-// face) base per row, so each cell's output lands at the reference position
-// base(x, y, seg) + running count.  Chunks whose activity bytes are all zero
-// are skipped without touching the volume, and a z step whose corners all lie
-// on one side of iso is dismissed with one warp-uniform test.
+// K3a compact.  Persistent warps walk the classify kernel's tiles (31 x-cells
+// by WY y-cells, one z segment), skipping z chunks whose activity bytes are
+// zero and z steps whose corners all lie on one side of iso.  Every active
+// cell gets one entry -- packed (x, y, z), case, its 8 corner values -- at
+// index base_a(piece) + running count, i.e. the list of active cells in the
+// reference's emission order.  Every 256th entry also records the global
+// vertex and face offsets of its cell.
 //
-// Emission.  Only ~1-6 % of cells produce output, so emitting from the walking
-// lanes would leave most of the warp idle.  Active cells are instead appended
-// (ballot + popc) to a per-warp queue in shared memory; once 32 or more are
-// queued the warp expands them into one task per output vertex and one per
-// face and runs those with all lanes busy.  Consecutive lanes then handle
-// consecutive vertices of a cell, so stores to the output are contiguous.
+// K3b expand.  Each CTA takes 256 consecutive entries, scans their vertex and
+// face counts, and turns them into one task per output vertex and one per
+// face.  Consecutive threads write consecutive vertices and faces, so the
+// mesh is stored with fully coalesced writes.
 //
 // Arithmetic follows Julia's promotion exactly (no FMA contraction):
 //   mu = (iso - v1) / (v2 - v1)         in Q (UInt16 differences wrap)
 //   p  = p1 + mu * (p2 - p1)             in P = promote(Q, eltype(LinRange))
 // then rounded to the output eltype.  On the two axes an edge does not move
 // along, p2 - p1 == 0 and the result is p1 itself unless p1 == 0 or mu is not
-// finite, in which case the literal expression is evaluated.
+// finite, in which case the literal expression is evaluated.  When P is
+// Float64 but mu and the output are Float32, the moving coordinate is
+// computed by the exact float path fast_f32_pos and only undecidable cases
+// fall back to FP64.
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
@@ -35,23 +37,9 @@ namespace mesh {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int U = 2;  // z planes loaded ahead (only active chunks are walked)
-constexpr int QFLUSH = 32;                  // expand once this many cells are queued
-constexpr int QCAP = QFLUSH + TILE_X;        // a row appends at most 31 cells before the next check
-
-// Per-warp queue of active cells of one tile (structure of arrays).
-template <class T> struct McQueue {
-    T val[8][QCAP];      // corner values, MC corner order
-    int32_t z[QCAP];
-    uint8_t lr[QCAP];    // lane | row << 5 (x = x0 + lane, y = y0 + row)
-    uint8_t cs[QCAP];
-    long long vb[QCAP], fb[QCAP];
-    int16_t vstart[QCAP], fstart[QCAP];
-    uint8_t vmap[QCAP * MC_MAX_VERTS];
-    uint8_t fmap[QCAP * MC_MAX_FACES];
-};
-static_assert(QCAP <= 256, "queue slots are addressed with uint8_t");
-constexpr size_t PLAN_BYTES = (sizeof(Plan) + 15) / 16 * 16;
+constexpr int U = 2;     // z planes loaded ahead (only active chunks are walked)
+constexpr int XW = 256;  // K3b threads per CTA == entries per block
+static_assert(XW == ENT_BLOCK, "one expansion CTA per block of entries");
 
 // MC edges (src/lut/mc.jl:606-608) on the corner order of src/marching_cubes.jl:111-120,
 // 9 bits per edge: a | b<<3 | moving axis<<6 | negative direction<<8; edges 0-5 in
@@ -71,19 +59,31 @@ __device__ __forceinline__ int cdx(int k) { return ((k + 1) >> 1) & 1; }
 __device__ __forceinline__ int cdy(int k) { return (k >> 1) & 1; }
 __device__ __forceinline__ int cdz(int k) { return (k >> 2) & 1; }
 
-// One output vertex: slot k of cell (x, y, z) with case cs, written to verts[out].
-// Written without lane-divergent branches except the rare literal p1 + mu*0.
+// p1 + mu*d in P, rounded to float: the literal evaluation, kept out of line so
+// that the rare cases that need it do not occupy the FP64 pipe for every vertex.
+template <class P> __device__ __noinline__ float moving_fp64(double c1, double d, double m) {
+    return (float)Ar<P>::add((P)c1, Ar<P>::mul((P)m, (P)d));
+}
+struct F3 {
+    float v[3];
+};
+template <class P> __device__ __noinline__ F3 still_fp64(const Plan *pp, int xa, int ya, int za, double m) {
+    const Plan &p = *pp;
+    F3 o;
+    o.v[0] = (float)Ar<P>::add(tab<P>(p.xp, p.xpf, xa), Ar<P>::mul((P)m, P(0)));
+    o.v[1] = (float)Ar<P>::add(tab<P>(p.yp, p.ypf, ya), Ar<P>::mul((P)m, P(0)));
+    o.v[2] = (float)Ar<P>::add(tab<P>(p.zp, p.zpf, za), Ar<P>::mul((P)m, P(0)));
+    return o;
+}
+
+// The vertex on MC edge e of cell (x, y, z) with corner values va (start) and
+// vbv (end), written to verts[out].
 template <class T, class Q, class P>
-__device__ __forceinline__ void vertex_task(const Plan &p, const uint64_t *s_v, const McQueue<T> &q, int j, int x,
-                                            int y, int z, int64_t out, int k) {
-    const int e = (int)((s_v[q.cs[j]] >> (4 * k)) & 15u);
+__device__ __forceinline__ void vertex_task(const Plan &p, int e, int x, int y, int z, T va, T vbv, int64_t out) {
     const int g = edge_info(e);
-    const int a = g & 7, b = (g >> 3) & 7, ax = (g >> 6) & 3, neg = (g >> 8) & 1;
+    const int a = g & 7, ax = (g >> 6) & 3, neg = (g >> 8) & 1;
     const int xa = x + cdx(a), ya = y + cdy(a), za = z + cdz(a);
-    const T va = q.val[a][j];
-    const T vbv = q.val[b][j];
     const Q mu = quotient<Q>(va, vbv, p);
-    const P m = (P)mu;
     // moving axis: p1 + mu * (+-(p[i+1] - p[i]))
     const int ia = ax == 0 ? xa : (ax == 1 ? ya : za);
     const double *tp = ax == 0 ? p.xp : (ax == 1 ? p.yp : p.zp);
@@ -91,9 +91,9 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const uint64_t *s_v, 
     const float *tpf = ax == 0 ? p.xpf : (ax == 1 ? p.ypf : p.zpf);
     const float *tdf = ax == 0 ? p.dxf : (ax == 1 ? p.dyf : p.dzf);
     const int id = neg ? ia - 1 : ia;
-    // still axes: p1 itself unless p1 == 0 or mu is not finite
     const bool fin = isfinite(mu);
     if (p.out64) {
+        const P m = (P)mu;
         const P c1 = tab<P>(tp, tpf, ia);
         const P d = tab<P>(td, tdf, id);
         const P rm = Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
@@ -107,11 +107,27 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const uint64_t *s_v, 
         o[0] = ax == 0 ? (double)rm : o0;
         o[1] = ax == 1 ? (double)rm : o1;
         o[2] = ax == 2 ? (double)rm : o2;
+    } else if (sizeof(P) == 4) {
+        const P m = (P)mu;
+        const P c1 = tab<P>(tp, tpf, ia);
+        const P d = tab<P>(td, tdf, id);
+        const float fr = (float)Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
+        float o0 = __ldg(p.xpf + xa), o1 = __ldg(p.ypf + ya), o2 = __ldg(p.zpf + za);
+        if (!fin || o0 == 0.0f || o1 == 0.0f || o2 == 0.0f) {
+            o0 = (float)Ar<P>::add((P)o0, Ar<P>::mul(m, P(0)));
+            o1 = (float)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
+            o2 = (float)Ar<P>::add((P)o2, Ar<P>::mul(m, P(0)));
+        }
+        float *o = (float *)p.verts + 3 * out;
+        o[0] = ax == 0 ? fr : o0;
+        o[1] = ax == 1 ? fr : o1;
+        o[2] = ax == 2 ? fr : o2;
     } else {
+        // Float64 positions rounded to Float32 output
         float fr;
         bool done = false;
-        if (sizeof(P) == 8 && sizeof(Q) == 4 && !p.force_fp64) {
-            // Float32 mu, Float64 coordinates, Float32 output: exact float fast path
+        if (sizeof(Q) == 4 && !p.force_fp64) {
+            // Float32 mu: exact float fast path
             const int64_t off = (ax == 0 ? 0 : (ax == 1 ? p.nx : p.nx + p.ny));
             const float *sp = p.split;
             const float dh = __ldg(sp + 2 * p.ntab + off + id), dl = __ldg(sp + 3 * p.ntab + off + id);
@@ -119,129 +135,41 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const uint64_t *s_v, 
                                        neg ? -dh : dh, neg ? -dl : dl, fr);
         }
         if (!done) {
-            const P c1 = tab<P>(tp, tpf, ia);
-            const P d = tab<P>(td, tdf, id);
-            fr = (float)Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
+            const double d = __ldg(td + id);
+            fr = moving_fp64<P>(__ldg(tp + ia), neg ? -d : d, (double)mu);
         }
-        float o0 = __ldg(p.xpf + xa), o1 = __ldg(p.ypf + ya), o2 = __ldg(p.zpf + za);
-        if (!fin || o0 == 0.0f || o1 == 0.0f || o2 == 0.0f) {
-            o0 = (float)Ar<P>::add(tab<P>(p.xp, p.xpf, xa), Ar<P>::mul(m, P(0)));
-            o1 = (float)Ar<P>::add(tab<P>(p.yp, p.ypf, ya), Ar<P>::mul(m, P(0)));
-            o2 = (float)Ar<P>::add(tab<P>(p.zp, p.zpf, za), Ar<P>::mul(m, P(0)));
-        }
+        F3 ov = {{__ldg(p.xpf + xa), __ldg(p.ypf + ya), __ldg(p.zpf + za)}};
+        if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f) ov = still_fp64<P>(&p, xa, ya, za, (double)mu);
         float *o = (float *)p.verts + 3 * out;
-        o[0] = ax == 0 ? fr : o0;
-        o[1] = ax == 1 ? fr : o1;
-        o[2] = ax == 2 ? fr : o2;
+        o[0] = ax == 0 ? fr : ov.v[0];
+        o[1] = ax == 1 ? fr : ov.v[1];
+        o[2] = ax == 2 ? fr : ov.v[2];
     }
 }
 
-// Expand the n queued cells of the tile at (x0, y0) into vertex and face tasks
-// and run them on all lanes.  Not inlined: the walk reaches it from several
-// unrolled sites.
-template <class T, class Q, class P>
-__device__ __noinline__ void flush(const Plan *pp, McQueue<T> *qp, int n, const uint64_t *s_v, const uint64_t *s_f,
-                                   int lane, int x0, int y0) {
-    const Plan &p = *pp;
-    McQueue<T> &q = *qp;
-    __syncwarp();
-    int nv = 0, nf = 0;
-    if (lane < n) {
-        const uint64_t t = s_v[q.cs[lane]];
-        nv = (int)((t >> 48) & 15u);
-        nf = (int)((t >> 52) & 7u);
-        if (q.vb[lane] + nv > p.verts_cap || q.fb[lane] + nf > p.faces_cap) {
-            atomicOr(p.err, ERR_CAPACITY);
-            nv = nf = 0;
-        }
-    }
-    int iv = nv, jf = nf;
+// 8 corner values of an entry, stored contiguously.
+template <class T> __device__ __forceinline__ void store8(T *dst, const T (&v)[8]) {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int a = __shfl_up_sync(FULL, iv, o), b = __shfl_up_sync(FULL, jf, o);
-        if (lane >= o) {
-            iv += a;
-            jf += b;
-        }
-    }
-    // second batch of entries (n <= QCAP < 64)
-    const int V0 = __shfl_sync(FULL, iv, 31), F0 = __shfl_sync(FULL, jf, 31);
-    int nv2 = 0, nf2 = 0;
-    const int j2 = lane + 32;
-    if (j2 < n) {
-        const uint64_t t = s_v[q.cs[j2]];
-        nv2 = (int)((t >> 48) & 15u);
-        nf2 = (int)((t >> 52) & 7u);
-        if (q.vb[j2] + nv2 > p.verts_cap || q.fb[j2] + nf2 > p.faces_cap) {
-            atomicOr(p.err, ERR_CAPACITY);
-            nv2 = nf2 = 0;
-        }
-    }
-    int iv2 = nv2, jf2 = nf2;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int a = __shfl_up_sync(FULL, iv2, o), b = __shfl_up_sync(FULL, jf2, o);
-        if (lane >= o) {
-            iv2 += a;
-            jf2 += b;
-        }
-    }
-    const int V = V0 + __shfl_sync(FULL, iv2, 31), F = F0 + __shfl_sync(FULL, jf2, 31);
-    if (lane < n) {
-        const int vs = iv - nv, fs = jf - nf;
-        q.vstart[lane] = (int16_t)vs;
-        q.fstart[lane] = (int16_t)fs;
-        for (int k = 0; k < nv; k++) q.vmap[vs + k] = (uint8_t)lane;
-        for (int k = 0; k < nf; k++) q.fmap[fs + k] = (uint8_t)lane;
-    }
-    if (j2 < n) {
-        const int vs = V0 + iv2 - nv2, fs = F0 + jf2 - nf2;
-        q.vstart[j2] = (int16_t)vs;
-        q.fstart[j2] = (int16_t)fs;
-        for (int k = 0; k < nv2; k++) q.vmap[vs + k] = (uint8_t)j2;
-        for (int k = 0; k < nf2; k++) q.fmap[fs + k] = (uint8_t)j2;
-    }
-    __syncwarp();
-    for (int t = lane; t < V; t += 32) {
-        const int j = q.vmap[t];
-        const int k = t - q.vstart[j];
-        const int lr = q.lr[j];
-        vertex_task<T, Q, P>(p, s_v, q, j, x0 + (lr & 31), y0 + (lr >> 5), q.z[j], q.vb[j] + k, k);
-    }
-    for (int t = lane; t < F; t += 32) {
-        const int j = q.fmap[t];
-        const int k = t - q.fstart[j];
-        const unsigned s = (unsigned)(s_f[q.cs[j]] >> (12 * k));
-        const int64_t vb = q.vb[j];
-        int64_t *o = p.faces + 3 * (q.fb[j] + k);
-        o[0] = vb + (s & 15u) + 1;
-        o[1] = vb + ((s >> 4) & 15u) + 1;
-        o[2] = vb + ((s >> 8) & 15u) + 1;
-    }
-    __syncwarp();
+    for (int k = 0; k < 8; k++) dst[k] = v[k];
+}
+template <> __device__ __forceinline__ void store8<float>(float *dst, const float (&v)[8]) {
+    float4 *d = reinterpret_cast<float4 *>(dst);
+    d[0] = make_float4(v[0], v[1], v[2], v[3]);
+    d[1] = make_float4(v[4], v[5], v[6], v[7]);
 }
 
-template <class T, class Q, class P>
-__global__ void __launch_bounds__(256, 3) k_emit_mc(const Plan p, int nitems) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint64_t *s_v = reinterpret_cast<uint64_t *>(smem);
-    uint64_t *s_f = s_v + 256;
-    Plan *s_plan = reinterpret_cast<Plan *>(s_f + 256);
-    McQueue<T> *queues = reinterpret_cast<McQueue<T> *>(smem + 2 * 256 * sizeof(uint64_t) + PLAN_BYTES);
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-        s_v[i] = MC_CASE_VERTS[i];
-        s_f[i] = MC_CASE_FACES[i];
-    }
-    if (threadIdx.x == 0) *s_plan = p;
+// ---------------------------------------------------------------- K3a ----
+
+template <class T>
+__global__ void __launch_bounds__(256) k_compact_mc(const Plan p, int nitems) {
+    __shared__ uint64_t s_v[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    McQueue<T> &q = queues[threadIdx.x >> 5];
     const T *vol = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
     const int64_t np = npieces(p);
-    const uint32_t lt = (1u << lane) - 1u;
-    int qn = 0;
 
     // persistent warps: take (y tile, x tile, segment) items in order from a counter
     for (;;) {
@@ -267,21 +195,21 @@ __global__ void __launch_bounds__(256, 3) k_emit_mc(const Plan p, int nitems) {
         }
         const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
         const uint32_t cellm = __ballot_sync(FULL, cellx);
-        int64_t bv[WY], bf[WY];
+        int64_t bv[WY], bf[WY], ba[WY];  // running vertex / face / entry offsets of each row's cell
 #pragma unroll
         for (int r = 0; r < WY; r++) {
-            bv[r] = bf[r] = 0;
+            bv[r] = bf[r] = ba[r] = 0;
             if (cellx && y0 + r < p.cy) {
                 const int64_t i = piece(p, seg, y0 + r, xs);
                 bv[r] = p.base[i];
                 bf[r] = p.base[np + i];
+                ba[r] = p.base[2 * np + i];
             }
         }
 
         uint32_t mlo[WY + 1];
         T lov[WY + 1];  // samples of plane z
         bool have_lo = false;
-        const int x0 = tx * TILE_X;
         for (int zc0 = zbeg; zc0 < zend; zc0 += ZC) {
             const int zc1 = min(zc0 + ZC, zend);
             const int chunk = seg * p.chunks_per_seg + (zc0 - zbeg) / ZC;
@@ -337,28 +265,25 @@ __global__ void __launch_bounds__(256, 3) k_emit_mc(const Plan p, int nitems) {
                                 const unsigned cm = (a & 1u) | ((a >> 1) << 1) | ((b >> 1) << 2) | ((b & 1u) << 3) |
                                                     ((c & 1u) << 4) | ((c >> 1) << 5) | ((d >> 1) << 6) |
                                                     ((d & 1u) << 7);
-                                const int slot = qn + __popc(actm & lt);
+                                const int64_t e = ba[r];
+                                if (e < p.ent_cap) {
+                                    p.ent_pos[e] = (unsigned long long)xs |
+                                                   ((unsigned long long)(y0 + r) << POS_BITS) |
+                                                   ((unsigned long long)zc << (2 * POS_BITS));
+                                    p.ent_cs[e] = (uint8_t)cm;
+                                    const T cv[8] = {a0, a1, b1, b0, c0, c1, d1, d0};
+                                    store8<T>((T *)p.ent_val + 8 * e, cv);
+                                    if ((e & (ENT_BLOCK - 1)) == 0) {
+                                        p.ent_side[2 * (e / ENT_BLOCK)] = bv[r];
+                                        p.ent_side[2 * (e / ENT_BLOCK) + 1] = bf[r];
+                                    }
+                                } else {
+                                    atomicOr(p.err, ERR_CAPACITY);
+                                }
                                 const uint64_t t = s_v[cm];
-                                q.val[0][slot] = a0;
-                                q.val[1][slot] = a1;
-                                q.val[2][slot] = b1;
-                                q.val[3][slot] = b0;
-                                q.val[4][slot] = c0;
-                                q.val[5][slot] = c1;
-                                q.val[6][slot] = d1;
-                                q.val[7][slot] = d0;
-                                q.z[slot] = zc;
-                                q.lr[slot] = (uint8_t)(lane | (r << 5));
-                                q.cs[slot] = (uint8_t)cm;
-                                q.vb[slot] = bv[r];
-                                q.fb[slot] = bf[r];
+                                ba[r] = e + 1;
                                 bv[r] += (int64_t)((t >> 48) & 15u);
                                 bf[r] += (int64_t)((t >> 52) & 7u);
-                            }
-                            qn += __popc(actm);
-                            if (qn >= QFLUSH) {
-                                flush<T, Q, P>(s_plan, &q, qn, s_v, s_f, lane, x0, y0);
-                                qn = 0;
                             }
                         }
                     }
@@ -369,17 +294,115 @@ __global__ void __launch_bounds__(256, 3) k_emit_mc(const Plan p, int nitems) {
                 for (int r = 0; r <= WY; r++) lov[r] = v[U - 1][r];
             }
         }
-        // the queue holds cells of this tile only
-        if (qn) {
-            flush<T, Q, P>(s_plan, &q, qn, s_v, s_f, lane, x0, y0);
-            qn = 0;
-        }
     }
 }
 
-int emit_grid(const void *fn, size_t smem, int sms) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * WARPS, smem) != cudaSuccess || per_sm < 1) {
+// ---------------------------------------------------------------- K3b ----
+
+template <class T> struct ExpandSmem {
+    T val[8][XW];
+    unsigned long long pos[XW];
+    int32_t vs[XW], fs[XW];
+    uint8_t cs[XW];
+    uint8_t vmap[XW * MC_MAX_VERTS];
+    uint8_t fmap[XW * MC_MAX_FACES];
+    int32_t wsum[2][XW / 32];
+};
+
+template <class T, class Q, class P>
+__global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
+    __shared__ uint64_t s_v[256], s_f[256];
+    __shared__ ExpandSmem<T> sm;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        s_v[i] = MC_CASE_VERTS[i];
+        s_f[i] = MC_CASE_FACES[i];
+    }
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t na = min(p.totals[2], p.ent_cap);
+    const int64_t nblocks = (na + XW - 1) / XW;
+    const uint64_t pmask = (1ull << POS_BITS) - 1;
+    __syncthreads();
+
+    for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+        const int64_t e = blk * XW + tid;
+        int nv = 0, nf = 0;
+        if (e < na) {
+            const int cs = p.ent_cs[e];
+            const uint64_t t = s_v[cs];
+            nv = (int)((t >> 48) & 15u);
+            nf = (int)((t >> 52) & 7u);
+            sm.cs[tid] = (uint8_t)cs;
+            sm.pos[tid] = p.ent_pos[e];
+            const T *src = (const T *)p.ent_val + 8 * e;
+#pragma unroll
+            for (int k = 0; k < 8; k++) sm.val[k][tid] = src[k];
+        }
+        // block exclusive scan of (nv, nf)
+        int iv = nv, jf = nf;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int a = __shfl_up_sync(FULL, iv, o), b = __shfl_up_sync(FULL, jf, o);
+            if (lane >= o) {
+                iv += a;
+                jf += b;
+            }
+        }
+        if (lane == 31) {
+            sm.wsum[0][w] = iv;
+            sm.wsum[1][w] = jf;
+        }
+        __syncthreads();
+        int wv = 0, wf = 0, V = 0, F = 0;
+#pragma unroll
+        for (int k = 0; k < XW / 32; k++) {
+            const int a = sm.wsum[0][k], b = sm.wsum[1][k];
+            if (k < w) {
+                wv += a;
+                wf += b;
+            }
+            V += a;
+            F += b;
+        }
+        const int vs = wv + iv - nv, fs = wf + jf - nf;
+        sm.vs[tid] = vs;
+        sm.fs[tid] = fs;
+        for (int k = 0; k < nv; k++) sm.vmap[vs + k] = (uint8_t)tid;
+        for (int k = 0; k < nf; k++) sm.fmap[fs + k] = (uint8_t)tid;
+        const int64_t vb0 = nblocks ? p.ent_side[2 * blk] : 0, fb0 = nblocks ? p.ent_side[2 * blk + 1] : 0;
+        __syncthreads();
+        if ((unsigned long long)(vb0 + V) > (unsigned long long)p.verts_cap ||
+            (unsigned long long)(fb0 + F) > (unsigned long long)p.faces_cap) {
+            if (tid == 0) atomicOr(p.err, ERR_CAPACITY);
+        } else {
+            for (int t = tid; t < V; t += XW) {
+                const int j = sm.vmap[t];
+                const int k = t - sm.vs[j];
+                const uint64_t pos = sm.pos[j];
+                const int ed = (int)((s_v[sm.cs[j]] >> (4 * k)) & 15u);
+                const int g = edge_info(ed);
+                vertex_task<T, Q, P>(p, ed, (int)(pos & pmask), (int)((pos >> POS_BITS) & pmask),
+                                     (int)(pos >> (2 * POS_BITS)), sm.val[g & 7][j], sm.val[(g >> 3) & 7][j], vb0 + t);
+            }
+            for (int t = tid; t < F; t += XW) {
+                const int j = sm.fmap[t];
+                const int k = t - sm.fs[j];
+                const unsigned s = (unsigned)(s_f[sm.cs[j]] >> (12 * k));
+                const int64_t vb = vb0 + sm.vs[j];
+                int64_t *o = p.faces + 3 * (fb0 + t);
+                o[0] = vb + (s & 15u) + 1;
+                o[1] = vb + ((s >> 4) & 15u) + 1;
+                o[2] = vb + ((s >> 8) & 15u) + 1;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+int resident_ctas(const void *fn, int threads) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
@@ -387,21 +410,17 @@ int emit_grid(const void *fn, size_t smem, int sms) {
 }
 
 template <class T, class Q, class P> cudaError_t go(const Plan &p, cudaStream_t s) {
-    const size_t sm = 2 * 256 * sizeof(uint64_t) + PLAN_BYTES + WARPS * sizeof(McQueue<T>);
-    static int grid = 0;  // per instantiation: resident CTAs on this device
-    if (!grid) {
-        cudaError_t e = cudaFuncSetAttribute(k_emit_mc<T, Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = emit_grid((const void *)k_emit_mc<T, Q, P>, sm, sms);
+    static int grid_a = 0, grid_b = 0;  // per instantiation: resident CTAs on this device
+    if (!grid_a) {
+        grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
+        grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P>, XW);
     }
     const int nitems = p.tiles_x * p.tiles_y * p.nseg;
     cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
-    const int ctas = std::min(grid, (nitems + WARPS - 1) / WARPS);
-    k_emit_mc<T, Q, P><<<ctas, 32 * WARPS, sm, s>>>(p, nitems);
+    k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_expand_mc<T, Q, P><<<grid_b, XW, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -10,7 +10,8 @@
 //
 // One CTA scans 32 columns (lane = x, so every access stays coalesced): its
 // 32 warps split the (y, seg) sequence of every column, reduce, scan across
-// warps through shared memory, scan the 32 column totals with warp shuffles,
+// warps through shared memory (one warp per counter: vertices, faces, active
+// cells), scan the 32 column totals with warp shuffles,
 // and chain the groups of 32 columns with a single-pass decoupled look-back
 // (groups are taken in ticket order, so every predecessor is already
 // resident).  Look-back waits are bounded: on expiry the kernel sets
@@ -66,8 +67,8 @@ __device__ int64_t look_back(unsigned long long *state, int tile, int64_t agg, i
 
 __global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
     __shared__ int s_tile;
-    __shared__ int64_t s_part[2][32][33];
-    __shared__ int64_t s_xpre[2][32];
+    __shared__ int64_t s_part[NCNT][32][33];
+    __shared__ int64_t s_xpre[NCNT][32];
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.scan_ticket, 1u);
     __syncthreads();
     const int tile = s_tile;
@@ -79,62 +80,59 @@ __global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
     const int64_t j0 = min(L, (int64_t)w * per), j1 = min(L, j0 + per);
     const int64_t np = npieces(p);
 
-    int64_t sv = 0, sf = 0;
+    int64_t sum[NCNT];
+#pragma unroll
+    for (int c = 0; c < NCNT; c++) sum[c] = 0;
     if (xok) {
         int y = (int)(j0 / p.nseg), seg = (int)(j0 % p.nseg);
         for (int64_t j = j0; j < j1; j++) {
             const int64_t i = piece(p, seg, y, x);
-            sv += p.cnt[i];
-            sf += p.cnt[np + i];
+#pragma unroll
+            for (int c = 0; c < NCNT; c++) sum[c] += p.cnt[c * np + i];
             if (++seg == p.nseg) { seg = 0; ++y; }
         }
     }
-    s_part[0][w][lane] = sv;
-    s_part[1][w][lane] = sf;
+#pragma unroll
+    for (int c = 0; c < NCNT; c++) s_part[c][w][lane] = sum[c];
     __syncthreads();
 
-    if (w == 0) {
-        int64_t tv = 0, tf = 0;  // column totals; s_part becomes the per-warp exclusive prefix
+    if (w < NCNT) {  // warp c scans counter c
+        const int c = w;
+        int64_t tot = 0;  // column total; s_part becomes the per-warp exclusive prefix
         for (int k = 0; k < 32; k++) {
-            const int64_t a = s_part[0][k][lane], b = s_part[1][k][lane];
-            s_part[0][k][lane] = tv;
-            s_part[1][k][lane] = tf;
-            tv += a;
-            tf += b;
+            const int64_t a = s_part[c][k][lane];
+            s_part[c][k][lane] = tot;
+            tot += a;
         }
-        int64_t iv = tv, jf = tf;  // inclusive scan across the 32 columns
+        int64_t inc = tot;  // inclusive scan across the 32 columns
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int64_t a = __shfl_up_sync(FULL, iv, o), b = __shfl_up_sync(FULL, jf, o);
-            if (lane >= o) { iv += a; jf += b; }
+            const int64_t a = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += a;
         }
-        const int64_t aggv = __shfl_sync(FULL, iv, 31), aggf = __shfl_sync(FULL, jf, 31);
-        int64_t pv = 0, pf = 0;
+        const int64_t agg = __shfl_sync(FULL, inc, 31);
+        int64_t pre = 0;
         if (lane == 0) {
-            pv = look_back(p.scan_state, tile, aggv, p.scan_spin_limit, p.err);
-            pf = look_back(p.scan_state + ntiles, tile, aggf, p.scan_spin_limit, p.err);
-            if (tile == ntiles - 1) {
-                p.totals[0] = pv + aggv;
-                p.totals[1] = pf + aggf;
-            }
+            pre = look_back(p.scan_state + (int64_t)c * ntiles, tile, agg, p.scan_spin_limit, p.err);
+            if (tile == ntiles - 1) p.totals[c] = pre + agg;
         }
-        pv = __shfl_sync(FULL, pv, 0);
-        pf = __shfl_sync(FULL, pf, 0);
-        s_xpre[0][lane] = pv + iv - tv;
-        s_xpre[1][lane] = pf + jf - tf;
+        pre = __shfl_sync(FULL, pre, 0);
+        s_xpre[c][lane] = pre + inc - tot;
     }
     __syncthreads();
 
     if (xok) {
-        int64_t bv = s_xpre[0][lane] + s_part[0][w][lane];
-        int64_t bf = s_xpre[1][lane] + s_part[1][w][lane];
+        int64_t b[NCNT];
+#pragma unroll
+        for (int c = 0; c < NCNT; c++) b[c] = s_xpre[c][lane] + s_part[c][w][lane];
         int y = (int)(j0 / p.nseg), seg = (int)(j0 % p.nseg);
         for (int64_t j = j0; j < j1; j++) {
             const int64_t i = piece(p, seg, y, x);
-            p.base[i] = bv;
-            p.base[np + i] = bf;
-            bv += p.cnt[i];
-            bf += p.cnt[np + i];
+#pragma unroll
+            for (int c = 0; c < NCNT; c++) {
+                p.base[c * np + i] = b[c];
+                b[c] += p.cnt[c * np + i];
+            }
             if (++seg == p.nseg) { seg = 0; ++y; }
         }
     }
@@ -146,7 +144,7 @@ int scan_tiles(const Plan &p) { return (p.cx + 31) / 32; }
 
 cudaError_t launch_scan(const Plan &p, cudaStream_t s) {
     const int ntiles = scan_tiles(p);
-    cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * 2 * (size_t)ntiles, s);
+    cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * NCNT * (size_t)ntiles, s);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(p.scan_ticket, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;

@@ -64,12 +64,12 @@ struct mesh_ctx {
     int sms = 148;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
-    DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f;
-    int64_t *h_misc = nullptr;  // pinned: totals[2], err
+    DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f, ent;
+    int64_t *h_misc = nullptr;  // pinned: totals[NCNT], err
     Plan plan{};
     int have_plan = 0;
     int Q64 = 0, A64 = 0, P64 = 0;
-    int64_t nverts = 0, nfaces = 0;
+    int64_t nverts = 0, nfaces = 0, nactive = 0;
     std::string msg;
     // stage timing (diagnostics)
     int timing = 0;
@@ -144,8 +144,8 @@ int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_
         if (!valid_scalar(p->range_type, p->range[i])) return fail(c, MESH_EINVAL, "range endpoint not representable");
     }
     if (nx < 0 || ny < 0 || nz < 0) return fail(c, MESH_EINVAL, "negative dimension");
-    const int64_t lim = (int64_t)1 << 30;
-    if (nx > lim || ny > lim || nz > lim) return fail(c, MESH_ETOOLARGE, "dimension above 2^30");
+    const int64_t lim = (int64_t)1 << POS_BITS;
+    if (nx > lim || ny > lim || nz > lim) return fail(c, MESH_ETOOLARGE, "dimension above 2^21");
     return MESH_OK;
 }
 
@@ -291,21 +291,22 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
 
     // scratch
     const int64_t np = npieces(P);
-    if ((e = c->cnt.ensure((size_t)np * 2 * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(c, e, "count buffer");
-    if ((e = c->base.ensure((size_t)np * 2 * sizeof(int64_t))) != cudaSuccess) return cuda_fail(c, e, "base buffer");
+    if ((e = c->cnt.ensure((size_t)np * NCNT * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(c, e, "count buffer");
+    if ((e = c->base.ensure((size_t)np * NCNT * sizeof(int64_t))) != cudaSuccess) return cuda_fail(c, e, "base buffer");
     const size_t fb = (size_t)P.nchunks * P.tiles_x * P.cy;
     if ((e = c->flags.ensure(fb)) != cudaSuccess) return cuda_fail(c, e, "flag buffer");
     const int st = scan_tiles(P);
-    if ((e = c->scan.ensure((size_t)st * 2 * sizeof(unsigned long long) + 64)) != cudaSuccess)
+    if ((e = c->scan.ensure((size_t)st * NCNT * sizeof(unsigned long long) + 64)) != cudaSuccess)
         return cuda_fail(c, e, "scan buffer");
     P.cnt = (uint32_t *)c->cnt.ptr;
     P.base = (int64_t *)c->base.ptr;
     P.flags = (uint8_t *)c->flags.ptr;
     P.scan_state = (unsigned long long *)c->scan.ptr;
-    P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + (size_t)st * 2 * sizeof(unsigned long long));
+    P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + (size_t)st * NCNT * sizeof(unsigned long long));
+    // misc: totals[NCNT] int64, then the error word and the work counter
     P.totals = (int64_t *)c->misc.ptr;
-    P.err = (unsigned int *)((int64_t *)c->misc.ptr + 2);
-    P.work = (unsigned int *)((int64_t *)c->misc.ptr + 3);
+    P.err = (unsigned int *)((int64_t *)c->misc.ptr + NCNT);
+    P.work = (unsigned int *)((int64_t *)c->misc.ptr + NCNT + 1);
     P.scan_spin_limit = 1 << 24;
     return MESH_OK;
 }
@@ -335,7 +336,8 @@ void mark(mesh_ctx *c, int stage) {
 int run_count(mesh_ctx *c) {
     Plan &P = c->plan;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(c->misc.ptr, 0, 32, c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
+    if ((e = cudaMemsetAsync(c->misc.ptr, 0, (NCNT + 2) * sizeof(int64_t), c->stream)) != cudaSuccess)
+        return cuda_fail(c, e, "memset");
     mark(c, 0);
     if ((e = launch_classify(P, c->stream)) != cudaSuccess) return cuda_fail(c, e, "classify launch");
     mark(c, 0);
@@ -346,7 +348,7 @@ int run_count(mesh_ctx *c) {
 }
 
 int check_err(mesh_ctx *c) {
-    const unsigned err = (unsigned)c->h_misc[2];
+    const unsigned err = (unsigned)c->h_misc[NCNT];
     if (err & ERR_SCAN_TIMEOUT) return fail(c, MESH_EDEVICE, "scan look-back wait expired");
     if (err & ERR_BOUNDS) return fail(c, MESH_EDEVICE, "device bounds check failed");
     if (err & ERR_CAPACITY) return fail(c, MESH_ECAPACITY, "output capacity too small");
@@ -354,10 +356,32 @@ int check_err(mesh_ctx *c) {
 }
 
 int fetch_misc(mesh_ctx *c) {
-    cudaError_t e = cudaMemcpyAsync(c->h_misc, c->misc.ptr, 3 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaMemcpyAsync(c->h_misc, c->misc.ptr, (NCNT + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "synchronize");
-    c->h_misc[2] &= 0xffffffffll;
+    c->h_misc[NCNT] &= 0xffffffffll;
+    return MESH_OK;
+}
+
+// Compact list of active cells (Marching Cubes), room for `cap` entries.
+int ensure_entries(mesh_ctx *c, int64_t cap) {
+    Plan &P = c->plan;
+    const size_t es = P.T == MESH_DT_U16 ? 2 : P.T == MESH_DT_F32 ? 4 : 8;
+    const int64_t nside = cap / ENT_BLOCK + 1;
+    auto up = [](size_t n) { return (n + 255) / 256 * 256; };  // every array 256-byte aligned
+    const size_t o_val = up((size_t)cap * 8);
+    const size_t o_side = o_val + up((size_t)cap * 8 * es);
+    const size_t o_cs = o_side + up((size_t)nside * 16);
+    const size_t bytes = o_cs + up((size_t)cap + 1);
+    cudaError_t e = c->ent.ensure(bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "entry buffer");
+    char *b = (char *)c->ent.ptr;
+    P.ent_pos = (unsigned long long *)b;
+    P.ent_val = b + o_val;  // 8 corner values per entry (vector stores need 16-byte alignment)
+    P.ent_side = (long long *)(b + o_side);
+    P.ent_cs = (uint8_t *)(b + o_cs);
+    P.ent_cap = cap;
     return MESH_OK;
 }
 
@@ -422,7 +446,7 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess ||
         c->misc.ensure(64) != cudaSuccess ||
-        cudaHostAlloc((void **)&c->h_misc, 4 * sizeof(int64_t), cudaHostAllocDefault) != cudaSuccess) {
+        cudaHostAlloc((void **)&c->h_misc, (NCNT + 2) * sizeof(int64_t), cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         mesh_ctx_destroy(c);
         return MESH_ENOMEM;
@@ -438,7 +462,7 @@ void mesh_ctx_destroy(mesh_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->vol, &c->tabs, &c->cnt, &c->base, &c->flags, &c->scan, &c->misc, &c->out_v, &c->out_f};
+    DevBuf *bufs[] = {&c->vol, &c->tabs, &c->cnt, &c->base, &c->flags, &c->scan, &c->misc, &c->out_v, &c->out_f, &c->ent};
     for (DevBuf *b : bufs) b->release();
     for (auto &v : c->ev_pairs)
         for (cudaEvent_t e : v) cudaEventDestroy(e);
@@ -486,6 +510,7 @@ int mesh_count(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int6
     if ((rc = check_err(c))) return rc;
     c->nverts = c->h_misc[0];
     c->nfaces = c->h_misc[1];
+    c->nactive = c->h_misc[2];
     *nverts = c->nverts;
     *nfaces = c->nfaces;
     c->have_plan = 1;
@@ -513,6 +538,7 @@ int mesh_fill(mesh_ctx *c, void *verts, int64_t *faces, int out_on_device) {
     P.verts_cap = c->nverts;
     P.faces_cap = c->nfaces;
     int rc;
+    if (P.alg == MESH_ALG_MC && (rc = ensure_entries(c, c->nactive))) return rc;
     if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
     if ((rc = launch_emit(c))) return rc;
     if (!out_on_device) {
@@ -547,6 +573,8 @@ int mesh_extract_device(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t
     P.faces = faces;
     P.verts_cap = verts ? verts_cap : 0;
     P.faces_cap = faces ? faces_cap : 0;
+    // an active Marching Cubes cell emits at least 3 vertices
+    if (P.alg == MESH_ALG_MC && (rc = ensure_entries(c, P.verts_cap / 3))) return rc;
     if ((rc = run_count(c))) return rc;
     if ((rc = launch_emit(c))) return rc;
     if ((e = cudaMemcpyAsync(counts, P.totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream)) !=

@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/meshing_gb300.h"
+#include "meshing_gb300.h"  // include/ (on the include path)
 
 namespace mesh {
 
@@ -17,6 +17,9 @@ constexpr int WARPS = 8;         // warps per CTA
 constexpr int TILE_X = 31;       // cells per tile in x (classify, MC emit)
 constexpr int TILE_XH = 30;      // cells per tile in x (MT / NSN emit, with -x halo)
 constexpr int ZC = 8;            // cells per activity chunk in z
+constexpr int NCNT = 3;          // per-piece counters: vertices, faces, active cells
+constexpr int ENT_BLOCK = 256;   // active-cell entries per expansion block
+constexpr int POS_BITS = 21;     // bits per coordinate in a packed cell position
 
 // Error bits of the device error word.
 constexpr unsigned ERR_SCAN_TIMEOUT = 1u;
@@ -57,14 +60,22 @@ struct Plan {
     int32_t zs, nseg, chunks_per_seg, nchunks;
     int32_t tiles_x, tiles_y;  // classify tiling (TILE_X x WY cells)
     // scratch
-    uint32_t *cnt;        // [2][nseg][cy][cx] per-piece vertex / face counts
-    int64_t *base;        // [2][nseg][cy][cx] exclusive prefix in traversal order
+    uint32_t *cnt;        // [NCNT][nseg][cy][cx] per-piece vertex / face / active-cell counts
+    int64_t *base;        // [NCNT][nseg][cy][cx] exclusive prefix in traversal order
     uint8_t *flags;       // [nchunks][tiles_x][cy] 1 if the tile row has an active cell
-    unsigned long long *scan_state;  // [2][scan tiles] decoupled look-back words
+    unsigned long long *scan_state;  // [NCNT][scan tiles] decoupled look-back words
     unsigned int *scan_ticket;
-    int64_t *totals;      // [2] total vertices, faces
+    int64_t *totals;      // [NCNT] total vertices, faces, active cells
     unsigned int *err;    // device error word
     unsigned int *work;   // work-item counter of the persistent kernels
+    // compact list of active cells in emission order (Marching Cubes):
+    // packed x | y << 21 | z << 42, case, the 8 corner values, and for every
+    // 256th entry the vertex / face offsets of that entry
+    unsigned long long *ent_pos;
+    uint8_t *ent_cs;
+    void *ent_val;
+    long long *ent_side;
+    int64_t ent_cap;
     // outputs
     void *verts;
     int64_t *faces;
