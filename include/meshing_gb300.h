@@ -54,7 +54,8 @@ typedef enum {
     MESH_EDEVICE = 4,      /* a kernel reported an error (bounded wait expired, bounds check) */
     MESH_ESTATE = 5,       /* mesh_fill without a preceding successful mesh_count */
     MESH_ECAPACITY = 6,    /* output buffers smaller than the mesh */
-    MESH_ETOOLARGE = 7     /* volume beyond the engine's index limits (more than 2^21 samples on an axis) */
+    MESH_ETOOLARGE = 7,    /* volume beyond the engine's index limits (more than 2^21 samples on an axis) */
+    MESH_ESCRATCH = 8      /* mesh_extract_noalloc: the call needs more than MESH_NOALLOC_SCRATCH_BYTES */
 } mesh_status;
 
 /* Mirrors MarchingCubes{T}(iso) / MarchingTetrahedra{T,E}(iso, eps) plus the
@@ -121,6 +122,29 @@ MESH_API int mesh_ctx_sync(mesh_ctx *ctx);
  * number of launches (launches[0..2]) since the previous query, then resets. */
 MESH_API int mesh_ctx_enable_timing(mesh_ctx *ctx, int enable);
 MESH_API int mesh_ctx_stage_times(mesh_ctx *ctx, double *ms, int64_t *launches);
+
+/* No counterpart in the reference.  Extraction for callers that must not
+ * allocate: code inside CUDA graph capture (cudaMalloc is illegal there),
+ * callbacks of a framework that owns the device memory pool, or real-time
+ * loops that must never wait on an allocator.  It does what
+ * mesh_extract_device does -- classify, scan, emit, asynchronously on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) -- but calls no
+ * allocating routine: the scratch it needs lives in one static device array of
+ * MESH_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits.  `vol`, `verts`, `faces` and `counts` are device memory
+ * owned by the caller; counts (int64[3]) receives nverts, nfaces and the
+ * device error bits (0 = complete; non-zero = outputs beyond verts_cap /
+ * faces_cap were not written).  Marching Cubes reserves room for verts_cap/3
+ * active cells, so its scratch grows with verts_cap; a call that needs more
+ * scratch than the limit returns MESH_ESCRATCH before any GPU work.  The first
+ * call on a device looks up the array's device address (once per device);
+ * make that first call before any stream capture.  All calls share the array
+ * and it keeps the last call's contents (each call clears what must start at
+ * zero), so calls that overlap on the GPU race: serialise them. */
+#define MESH_NOALLOC_SCRATCH_BYTES (64ull << 20)
+MESH_API int mesh_extract_noalloc(const void *vol, int vol_dtype, int64_t nx, int64_t ny, int64_t nz,
+                                  const mesh_params *p, void *verts, int64_t verts_cap, int64_t *faces,
+                                  int64_t faces_cap, int64_t *counts, void *stream);
 
 #ifdef __cplusplus
 }

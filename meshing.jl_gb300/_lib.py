@@ -12,12 +12,12 @@ LIB_PATH = os.path.join(HERE, '_build', 'libmeshing_gb300.so')
 MESH_DT_U16, MESH_DT_F32, MESH_DT_F64, MESH_DT_I64 = 1, 2, 3, 4
 MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN = 0, 1, 2
 STATUS = {0: 'MESH_OK', 1: 'MESH_EINVAL', 2: 'MESH_ENOMEM', 3: 'MESH_ECUDA', 4: 'MESH_EDEVICE', 5: 'MESH_ESTATE',
-          6: 'MESH_ECAPACITY', 7: 'MESH_ETOOLARGE'}
+          6: 'MESH_ECAPACITY', 7: 'MESH_ETOOLARGE', 8: 'MESH_ESCRATCH'}
 
 # every symbol the header declares
 EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_ctx_set_stream', 'mesh_status_string',
            'mesh_ctx_last_error', 'mesh_output_float_bits', 'mesh_count', 'mesh_fill', 'mesh_extract_device',
-           'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times')
+           'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times', 'mesh_extract_noalloc')
 
 
 class MeshParams(ctypes.Structure):
@@ -59,6 +59,7 @@ def load():
         'mesh_ctx_sync': (c_int, [vp]),
         'mesh_ctx_enable_timing': (c_int, [vp, c_int]),
         'mesh_ctx_stage_times': (c_int, [vp, P(ctypes.c_double), P(i64)]),
+        'mesh_extract_noalloc': (c_int, [vp, c_int, i64, i64, i64, P(MeshParams), vp, i64, vp, i64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

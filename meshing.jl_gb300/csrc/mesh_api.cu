@@ -424,6 +424,7 @@ const char *mesh_status_string(int s) {
     case MESH_ESTATE: return "mesh_fill called without a successful mesh_count";
     case MESH_ECAPACITY: return "output capacity too small";
     case MESH_ETOOLARGE: return "volume too large";
+    case MESH_ESCRATCH: return "needs more scratch than the no-allocation limit";
     default: return "unknown status";
     }
 }
