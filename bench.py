@@ -250,10 +250,21 @@ def run_ours(args, rank, world, dist):
     in_b = vox * 4
     out_b = nv * 12 + nf * 24
     stage = {k: v[0] / max(v[1], 1) for k, v in st.items()}
-    # algorithmic bytes per launch: classify reads the volume once; emit writes the mesh
-    alg_bytes = {'classify': in_b, 'scan': (n - 1) ** 2 * 2 * (4 + 8) * 1.0, 'emit': out_b}
-    dom = max(stage, key=stage.get)
-    achieved = alg_bytes[dom] / (stage[dom] * 1e-3) / 1e9
+    # algorithmic bytes per launch: classify reads every sample once (4 B); the emit
+    # stage (active-cell compaction + expansion) writes the mesh (12 B per vertex,
+    # 24 B per face); the scan reads 3 u32 counts and writes 3 int64 bases per piece
+    emit_ms = stage['emit'] + stage['expand']
+    kern = {
+        'classify': {'ms': stage['classify'], 'bytes': in_b},
+        'scan': {'ms': stage['scan'], 'bytes': float((n - 1) ** 2 * 3 * (4 + 8))},
+        'emit': {'ms': emit_ms, 'bytes': float(out_b), 'launches': ['compact', 'expand'],
+                 'compact_ms': stage['emit'], 'expand_ms': stage['expand']},
+    }
+    for k in kern.values():
+        k['gbs'] = k['bytes'] / (k['ms'] * 1e-3) / 1e9 if k['ms'] else None
+        k['frac'] = k['gbs'] / peak if k['gbs'] else None
+    dom = 'classify' if kern['classify']['ms'] >= kern['emit']['ms'] else 'emit'
+    achieved = kern[dom]['gbs']
     traffic = None
     tpath = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tpath):
@@ -280,7 +291,8 @@ def run_ours(args, rank, world, dist):
                    'stage_ms': stage, 'e2e_matches_device': bool(ok)},
         'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'traffic': traffic, 'peak_source': peak_kind,
-                     'algorithmic_bytes': alg_bytes[dom]},
+                     'algorithmic_bytes': kern[dom]['bytes']},
+        'kernels': kern,
         'pipeline': {'bytes': in_b + out_b, 'achieved': pipe_gbs, 'frac': pipe_gbs / peak, 'unit': 'GB/s'},
         'e2e': {'value': vox * world / (e2e_ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': e2e_ms,
                 'h2d_bytes_per_step': int(in_b), 'd2h_bytes_per_step': int(out_b)},

@@ -116,10 +116,12 @@ MESH_API int mesh_extract_device(mesh_ctx *ctx, const void *vol, int vol_dtype, 
 MESH_API int mesh_ctx_sync(mesh_ctx *ctx);
 
 /* Diagnostics (no counterpart in the reference, which has no instrumentation):
- * with timing enabled the context brackets every classify, scan and emit
- * launch with CUDA events on its stream.  mesh_ctx_stage_times waits for them
- * and returns, per stage, the summed device milliseconds (ms[0..2]) and the
- * number of launches (launches[0..2]) since the previous query, then resets. */
+ * with timing enabled the context brackets every kernel launch with CUDA
+ * events on its stream.  mesh_ctx_stage_times waits for them and returns, per
+ * stage -- 0 classify, 1 scan, 2 emit (the Marching Cubes active-cell
+ * compaction, or the whole MT / NSN emit), 3 Marching Cubes expansion -- the
+ * summed device milliseconds ms[0..3] and the number of kernel launches
+ * launches[0..3] since the previous query, then resets. */
 MESH_API int mesh_ctx_enable_timing(mesh_ctx *ctx, int enable);
 MESH_API int mesh_ctx_stage_times(mesh_ctx *ctx, double *ms, int64_t *launches);
 

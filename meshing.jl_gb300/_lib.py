@@ -103,11 +103,12 @@ class Context:
         check(self._lib.mesh_ctx_enable_timing(self.handle, 1 if on else 0), self.handle)
 
     def stage_times(self):
-        """{'classify'|'scan'|'emit': (total device ms, launches)} since the last query."""
-        ms = (ctypes.c_double * 3)()
-        n = (ctypes.c_int64 * 3)()
+        """{stage: (total device ms, kernel launches)} since the last query; stages are
+        classify, scan, emit (MC active-cell compaction, or the whole MT/NSN emit), expand."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_int64 * 4)()
         check(self._lib.mesh_ctx_stage_times(self.handle, ms, n), self.handle)
-        return {k: (ms[i], n[i]) for i, k in enumerate(('classify', 'scan', 'emit'))}
+        return {k: (ms[i], n[i]) for i, k in enumerate(('classify', 'scan', 'emit', 'expand'))}
 
     def sync(self):
         check(self._lib.mesh_ctx_sync(self.handle), self.handle)

@@ -14,6 +14,7 @@
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
+#include "mesh_tma.cuh"
 
 namespace mesh {
 
@@ -34,9 +35,7 @@ __device__ __forceinline__ unsigned mt_case(unsigned a, unsigned b, unsigned c, 
            ((d >> 1) << 6) | ((c >> 1) << 7);
 }
 
-template <class T, int ALG>
-__global__ void __launch_bounds__(256) k_classify(const Plan p) {
-    __shared__ uint32_t s_tab[256];
+template <int ALG> __device__ __forceinline__ void load_tables(uint32_t *s_tab) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
         if (ALG == MESH_ALG_MC) {
             uint64_t t = MC_CASE_VERTS[i];
@@ -45,6 +44,97 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
             s_tab[i] = MT_TOUCHED[i] | ((uint32_t)MT_CASE_NFACES[i] << 24);
         }
     }
+}
+
+// Per-lane running counts of the WY cells (rows) a lane owns, and per-row
+// activity of the current z chunk (warp-uniform).
+struct Counts {
+    uint32_t v[WY], f[WY], a[WY], act[WY];
+};
+
+// One z step: the cells between the sample planes whose row masks are mlo
+// (plane z) and mhi (plane z+1).
+template <int ALG>
+__device__ __forceinline__ void step(const Plan &p, const uint32_t *s_tab, const uint32_t (&mlo)[WY + 1],
+                                     const uint32_t (&mhi)[WY + 1], uint32_t xval, uint32_t cellm, int lane, int xs,
+                                     int y0, int zc, Counts &c) {
+    uint32_t all1 = xval, any1 = 0;
+#pragma unroll
+    for (int r = 0; r <= WY; r++) {
+        all1 &= mlo[r] & mhi[r];
+        any1 |= mlo[r] | mhi[r];
+    }
+    // warp-uniform early out: every corner of every cell in this step on one side
+    if (all1 == xval || any1 == 0) return;
+#pragma unroll
+    for (int r = 0; r < WY; r++) {
+        // bit l: cell l has corners on both sides (bits l, l+1 of the four masks)
+        const uint32_t and4 = mlo[r] & mlo[r + 1] & mhi[r] & mhi[r + 1];
+        const uint32_t or4 = mlo[r] | mlo[r + 1] | mhi[r] | mhi[r + 1];
+        const uint32_t actm = (or4 | (or4 >> 1)) & ~(and4 & (and4 >> 1)) & cellm;
+        if (actm == 0u || y0 + r >= p.cy) continue;  // warp-uniform
+        c.act[r] = 1;
+        if (!((actm >> lane) & 1u)) continue;
+        c.a[r] += 1;
+        const unsigned a = (mlo[r] >> lane) & 3u, b = (mlo[r + 1] >> lane) & 3u;
+        const unsigned cc = (mhi[r] >> lane) & 3u, d = (mhi[r + 1] >> lane) & 3u;
+        const unsigned cm = mc_case(a, b, cc, d);
+        if (ALG == MESH_ALG_MC) {
+            const uint32_t t = s_tab[cm];
+            c.v[r] += t & 15u;
+            c.f[r] += t >> 8;
+        } else if (ALG == MESH_ALG_MT) {
+            const uint32_t t = s_tab[mt_case(a, b, cc, d)];
+            const int bnd = (xs == 0) | ((y0 + r == 0) << 1) | ((zc == 0) << 2);
+            c.v[r] += __popc(t & p.own[bnd] & 0x7ffffu);
+            c.f[r] += t >> 24;
+        } else {  // NSN: one vertex per active cell, a quad per crossed base edge
+            c.v[r] += 1;
+            const unsigned s0 = cm & 1u;
+            const bool yk = y0 + r > 0, zk = zc > 0, xk = xs > 0;
+            unsigned q = 0;
+            q += (s0 != ((cm >> 1) & 1u)) && yk && zk;  // +x edge
+            q += (s0 != ((cm >> 3) & 1u)) && zk && xk;  // +y edge
+            q += (s0 != ((cm >> 4) & 1u)) && xk && yk;  // +z edge
+            c.f[r] += 2 * q;
+        }
+    }
+}
+
+// At the end of an activity chunk: publish one byte per tile row.
+__device__ __forceinline__ void chunk_end(const Plan &p, int lane, int tx, int y0, int seg, int zbeg, int zc,
+                                          int zend, Counts &c) {
+    if (((zc + 1 - zbeg) % ZC) == 0 || zc + 1 == zend) {
+        const int chunk = seg * p.chunks_per_seg + (zc - zbeg) / ZC;
+        uint8_t mine = 0;
+#pragma unroll
+        for (int r = 0; r < WY; r++) {
+            if (lane == r) mine = c.act[r] != 0;  // act[] is warp-uniform
+            c.act[r] = 0;
+        }
+        if (lane < WY && y0 + lane < p.cy) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+    }
+}
+
+__device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, int y0, int seg, const Counts &c) {
+    if (!cellx) return;
+    const int64_t np = npieces(p);
+#pragma unroll
+    for (int r = 0; r < WY; r++) {
+        if (y0 + r < p.cy) {
+            const int64_t i = piece(p, seg, y0 + r, xs);
+            p.cnt[i] = c.v[r];
+            p.cnt[np + i] = c.f[r];
+            p.cnt[2 * np + i] = c.a[r];
+        }
+    }
+}
+
+// Walk with one coalesced global load per lane, row and plane (any layout).
+template <class T, int ALG>
+__global__ void __launch_bounds__(256) k_classify(const Plan p) {
+    __shared__ uint32_t s_tab[256];
+    load_tables<ALG>(s_tab);
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -67,11 +157,9 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
         rowok[r] = xs < p.nx && y0 + r < p.ny;
         rowp[r] = rowok[r] ? vol + xs + p.nx * (int64_t)(y0 + r) : vol;
     }
-
-    uint32_t cntv[WY], cntf[WY], cnta[WY], act[WY];
+    Counts c;
 #pragma unroll
-    for (int r = 0; r < WY; r++) cntv[r] = cntf[r] = cnta[r] = act[r] = 0;
-
+    for (int r = 0; r < WY; r++) c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
     // lanes whose sample exists (x < nx): only their bits take part in the uniform test
     const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
     const uint32_t cellm = __ballot_sync(FULL, cellx);
@@ -102,78 +190,132 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
             const int zc = z + u;
             if (zc >= zend) break;  // warp-uniform
             uint32_t mhi[WY + 1];
-            uint32_t all1 = xval, any1 = 0;
 #pragma unroll
-            for (int r = 0; r <= WY; r++) {
-                mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
-                all1 &= mlo[r] & mhi[r];
-                any1 |= mlo[r] | mhi[r];
-            }
-            // warp-uniform early out: every corner of every cell in this step on one side
-            if (all1 != xval && any1 != 0) {
-#pragma unroll
-                for (int r = 0; r < WY; r++) {
-                    // bit l: cell l has corners on both sides (bits l, l+1 of the four masks)
-                    const uint32_t and4 = mlo[r] & mlo[r + 1] & mhi[r] & mhi[r + 1];
-                    const uint32_t or4 = mlo[r] | mlo[r + 1] | mhi[r] | mhi[r + 1];
-                    const uint32_t actm = (or4 | (or4 >> 1)) & ~(and4 & (and4 >> 1)) & cellm;
-                    if (actm == 0u || y0 + r >= p.cy) continue;  // warp-uniform
-                    act[r] = 1;
-                    if (!((actm >> lane) & 1u)) continue;
-                    cnta[r] += 1;
-                    const unsigned a = (mlo[r] >> lane) & 3u, b = (mlo[r + 1] >> lane) & 3u;
-                    const unsigned c = (mhi[r] >> lane) & 3u, d = (mhi[r + 1] >> lane) & 3u;
-                    const unsigned cm = mc_case(a, b, c, d);
-                    if (ALG == MESH_ALG_MC) {
-                        const uint32_t t = s_tab[cm];
-                        cntv[r] += t & 15u;
-                        cntf[r] += t >> 8;
-                    } else if (ALG == MESH_ALG_MT) {
-                        const uint32_t t = s_tab[mt_case(a, b, c, d)];
-                        const int bnd = (xs == 0) | ((y0 + r == 0) << 1) | ((zc == 0) << 2);
-                        cntv[r] += __popc(t & p.own[bnd] & 0x7ffffu);
-                        cntf[r] += t >> 24;
-                    } else {  // NSN: one vertex per active cell, a quad per crossed base edge
-                        cntv[r] += 1;
-                        const unsigned s0 = cm & 1u;
-                        const bool yk = y0 + r > 0, zk = zc > 0, xk = xs > 0;
-                        unsigned q = 0;
-                        q += (s0 != ((cm >> 1) & 1u)) && yk && zk;  // +x edge
-                        q += (s0 != ((cm >> 3) & 1u)) && zk && xk;  // +y edge
-                        q += (s0 != ((cm >> 4) & 1u)) && xk && yk;  // +z edge
-                        cntf[r] += 2 * q;
-                    }
-                }
-            }
+            for (int r = 0; r <= WY; r++) mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
+            step<ALG>(p, s_tab, mlo, mhi, xval, cellm, lane, xs, y0, zc, c);
 #pragma unroll
             for (int r = 0; r <= WY; r++) mlo[r] = mhi[r];
-            // end of an activity chunk: publish one byte per tile row
-            if (((zc + 1 - zbeg) % ZC) == 0 || zc + 1 == zend) {
-                const int chunk = seg * p.chunks_per_seg + (zc - zbeg) / ZC;
-                uint8_t mine = 0;
-#pragma unroll
-                for (int r = 0; r < WY; r++) {
-                    if (lane == r) mine = act[r] != 0;  // act[] is warp-uniform
-                    act[r] = 0;
-                }
-                if (lane < WY && y0 + lane < p.cy)
-                    p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
-            }
+            chunk_end(p, lane, tx, y0, seg, zbeg, zc, zend, c);
         }
     }
+    store_counts(p, cellx, xs, y0, seg, c);
+}
 
-    if (cellx) {
-        const int64_t np = npieces(p);
-#pragma unroll
-        for (int r = 0; r < WY; r++) {
-            if (y0 + r < p.cy) {
-                const int64_t i = piece(p, seg, y0 + r, xs);
-                p.cnt[i] = cntv[r];
-                p.cnt[np + i] = cntf[r];
-                p.cnt[2 * np + i] = cnta[r];
-            }
+// Walk over TMA-staged bricks.  The CTA's 31 x 32 cells of a z segment are
+// streamed as boxes of TMA_BZ planes x 33 rows x BX samples through a ring of
+// TMA_STAGES shared-memory stages.  Warp specialisation: warp WARPS (the
+// producer) issues cp.async.bulk.tensor into a free stage and arms its `full`
+// mbarrier with the byte count; the WARPS consumer warps wait on `full`,
+// classify their 4 cell rows, and release the stage by arriving on its
+// `empty` mbarrier.  The box starts on the 16-byte boundary at or below the
+// tile's first sample; lanes index from the remainder.  Needs rows whose byte
+// stride is a multiple of 16.  All waits are bounded; on expiry the CTA
+// reports ERR_TMA_TIMEOUT, waits (bounded) for its copies in flight and exits.
+template <class T, int ALG>
+__global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p, const __grid_constant__ CUtensorMap tmap) {
+    constexpr int BX = TmaBox<T>::BX, AL = TmaBox<T>::ALIGN;
+    constexpr int PLANE = TMA_BY * BX;
+    constexpr unsigned BYTES = TMA_BZ * PLANE * sizeof(T);         // one box
+    constexpr int STAGE = (int)(tma_stage_bytes<T>() / sizeof(T));  // stage stride, 128-byte aligned
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *buf = reinterpret_cast<T *>(smem_raw);  // [TMA_STAGES][STAGE]
+    __shared__ uint32_t s_tab[256];
+    __shared__ __align__(8) uint64_t full[TMA_STAGES], empty[TMA_STAGES];
+    __shared__ int s_fail;
+    load_tables<ALG>(s_tab);
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int tx = blockIdx.x, seg = blockIdx.z;
+    const int x0 = tx * TILE_X, xa = x0 & ~(AL - 1), xoff = x0 - xa;
+    const int yc0 = blockIdx.y * WARPS * WY;
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    const int nst = (zend - zbeg + 1 + TMA_BZ - 1) / TMA_BZ;  // planes zbeg..zend
+
+    if (tid == 0) {
+        for (int k = 0; k < TMA_STAGES; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], WARPS);
         }
+        s_fail = 0;
+        mbar_fence_init();
     }
+    __syncthreads();
+
+    if (w == WARPS) {  // producer
+        int issued = 0;
+        if (lane == 0) {
+            for (int s = 0; s < nst; s++) {
+                const int slot = s % TMA_STAGES;
+                if (s >= TMA_STAGES && !mbar_wait(&empty[slot], (unsigned)(s / TMA_STAGES - 1) & 1u)) {
+                    atomicOr(&s_fail, 1);
+                    break;
+                }
+                if (*(volatile int *)&s_fail) break;
+                fence_proxy_async();
+                mbar_expect_tx(&full[slot], BYTES);
+                tma_load_3d(buf + slot * STAGE, &tmap, xa, yc0, zbeg + s * TMA_BZ, &full[slot]);
+                issued = s + 1;
+            }
+            // on failure, let the copies in flight land before the CTA exits
+            if (*(volatile int *)&s_fail)
+                for (int s = max(0, issued - TMA_STAGES); s < issued; s++)
+                    mbar_wait(&full[s % TMA_STAGES], (unsigned)(s / TMA_STAGES) & 1u);
+        }
+        __syncwarp();
+    } else {  // consumers
+        const int ty = blockIdx.y * WARPS + w;
+        const int y0 = ty * WY;
+        const bool warp_on = ty < p.tiles_y;
+        const int xs = x0 + lane;
+        const bool cellx = lane < TILE_X && xs < p.cx;
+        bool rowok[WY + 1];
+#pragma unroll
+        for (int r = 0; r <= WY; r++) rowok[r] = xs < p.nx && y0 + r < p.ny;
+        Counts c;
+#pragma unroll
+        for (int r = 0; r < WY; r++) c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
+        const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
+        const uint32_t cellm = __ballot_sync(FULL, cellx);
+        uint32_t mlo[WY + 1];
+#pragma unroll
+        for (int r = 0; r <= WY; r++) mlo[r] = 0;
+        bool ok = true;
+        for (int s = 0; s < nst; s++) {
+            const int slot = s % TMA_STAGES;
+            ok = mbar_wait(&full[slot], (unsigned)(s / TMA_STAGES) & 1u);
+            ok = __all_sync(FULL, ok) && !*(volatile int *)&s_fail;
+            if (!ok) {
+                if (lane == 0) atomicOr(&s_fail, 1);
+                break;
+            }
+            const T *st = buf + slot * STAGE;
+            if (warp_on) {
+#pragma unroll
+                for (int k = 0; k < TMA_BZ; k++) {
+                    const int plane = zbeg + s * TMA_BZ + k;
+                    if (plane > zend) break;  // warp-uniform
+                    uint32_t m[WY + 1];
+#pragma unroll
+                    for (int r = 0; r <= WY; r++)
+                        m[r] = __ballot_sync(FULL,
+                                             rowok[r] && below(st[k * PLANE + (w * WY + r) * BX + xoff + lane], p));
+                    if (plane > zbeg) {
+                        const int zc = plane - 1;
+                        step<ALG>(p, s_tab, mlo, m, xval, cellm, lane, xs, y0, zc, c);
+                        chunk_end(p, lane, tx, y0, seg, zbeg, zc, zend, c);
+                    }
+#pragma unroll
+                    for (int r = 0; r <= WY; r++) mlo[r] = m[r];
+                }
+            }
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&empty[slot])) : "memory");
+        }
+        if (ok && warp_on) store_counts(p, cellx, xs, y0, seg, c);
+    }
+    __syncthreads();
+    if (tid == 0 && s_fail) atomicOr(p.err, ERR_TMA_TIMEOUT);
 }
 
 template <class T> cudaError_t launch_t(const Plan &p, cudaStream_t s) {
@@ -186,7 +328,36 @@ template <class T> cudaError_t launch_t(const Plan &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <class T> cudaError_t launch_tma_t(const Plan &p, const CUtensorMap &map, cudaStream_t s) {
+    dim3 grid(p.tiles_x, (p.tiles_y + WARPS - 1) / WARPS, p.nseg);
+    const size_t sm = (size_t)TMA_STAGES * tma_stage_bytes<T>();
+    cudaError_t e = cudaSuccess;
+    switch (p.alg) {
+    case MESH_ALG_MC:
+        e = cudaFuncSetAttribute(k_classify_tma<T, MESH_ALG_MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess) k_classify_tma<T, MESH_ALG_MC><<<grid, 32 * (WARPS + 1), sm, s>>>(p, map);
+        break;
+    case MESH_ALG_MT:
+        e = cudaFuncSetAttribute(k_classify_tma<T, MESH_ALG_MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess) k_classify_tma<T, MESH_ALG_MT><<<grid, 32 * (WARPS + 1), sm, s>>>(p, map);
+        break;
+    default:
+        e = cudaFuncSetAttribute(k_classify_tma<T, MESH_ALG_NSN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess) k_classify_tma<T, MESH_ALG_NSN><<<grid, 32 * (WARPS + 1), sm, s>>>(p, map);
+        break;
+    }
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_classify_tma(const Plan &p, const CUtensorMap &map, cudaStream_t s) {
+    switch (p.T) {
+    case MESH_DT_U16: return launch_tma_t<uint16_t>(p, map, s);
+    case MESH_DT_F32: return launch_tma_t<float>(p, map, s);
+    default: return launch_tma_t<double>(p, map, s);
+    }
+}
 
 cudaError_t launch_classify(const Plan &p, cudaStream_t s) {
     switch (p.T) {

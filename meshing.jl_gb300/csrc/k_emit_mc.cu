@@ -161,7 +161,7 @@ template <> __device__ __forceinline__ void store8<float>(float *dst, const floa
 // ---------------------------------------------------------------- K3a ----
 
 template <class T>
-__global__ void __launch_bounds__(256) k_compact_mc(const Plan p, int nitems) {
+__global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems) {
     __shared__ uint64_t s_v[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
     __syncthreads();
@@ -409,34 +409,37 @@ int resident_ctas(const void *fn, int threads) {
     return per_sm * sms;
 }
 
-template <class T, class Q, class P> cudaError_t go(const Plan &p, cudaStream_t s) {
+template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cudaStream_t s) {
     static int grid_a = 0, grid_b = 0;  // per instantiation: resident CTAs on this device
     if (!grid_a) {
         grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
         grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P>, XW);
     }
-    const int nitems = p.tiles_x * p.tiles_y * p.nseg;
-    cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
-    k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_expand_mc<T, Q, P><<<grid_b, XW, 0, s>>>(p);
+    if (stage == 0) {
+        const int nitems = p.tiles_x * p.tiles_y * p.nseg;
+        cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+        k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);
+    } else {
+        k_expand_mc<T, Q, P><<<grid_b, XW, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
-template <class T> cudaError_t go_t(const Plan &p, int Q64, int P64, cudaStream_t s) {
-    if (Q64) return go<T, double, double>(p, s);
-    if (P64) return go<T, float, double>(p, s);
-    return go<T, float, float>(p, s);
+template <class T> cudaError_t go_t(const Plan &p, int Q64, int P64, int stage, cudaStream_t s) {
+    if (Q64) return go<T, double, double>(p, stage, s);
+    if (P64) return go<T, float, double>(p, stage, s);
+    return go<T, float, float>(p, stage, s);
 }
 
 }  // namespace
 
-cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, cudaStream_t s) {
+// stage 0: K3a compact (active-cell list); stage 1: K3b expand (vertices and faces)
+cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStream_t s) {
     switch (p.T) {
-    case MESH_DT_U16: return go_t<uint16_t>(p, Q64, P64, s);
-    case MESH_DT_F32: return go_t<float>(p, Q64, P64, s);
-    default: return go<double, double, double>(p, s);
+    case MESH_DT_U16: return go_t<uint16_t>(p, Q64, P64, stage, s);
+    case MESH_DT_F32: return go_t<float>(p, Q64, P64, stage, s);
+    default: return go<double, double, double>(p, stage, s);
     }
 }
 

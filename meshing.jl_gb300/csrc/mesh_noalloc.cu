@@ -28,7 +28,7 @@
 #include "mesh_tables.h"
 
 namespace mesh {
-cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, cudaStream_t s);
+cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStream_t s);
 cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
 int scan_tiles(const Plan &p);
 }  // namespace mesh
@@ -229,8 +229,12 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     if ((e = cudaGetLastError()) != cudaSuccess) return MESH_ECUDA;
     if ((e = launch_classify(P, s)) != cudaSuccess) return MESH_ECUDA;
     if ((e = launch_scan(P, s)) != cudaSuccess) return MESH_ECUDA;
-    if (P.alg == MESH_ALG_MC) e = launch_emit_mc(P, Q64, P64, s);
-    else e = launch_emit_halo(P, Q64, A64, P64, s);
+    if (P.alg == MESH_ALG_MC) {
+        e = launch_emit_mc(P, Q64, P64, 0, s);
+        if (e == cudaSuccess) e = launch_emit_mc(P, Q64, P64, 1, s);
+    } else {
+        e = launch_emit_halo(P, Q64, A64, P64, s);
+    }
     if (e != cudaSuccess) return MESH_ECUDA;
     // counts[0..1] = totals; counts[2] = device error bits (0 when the outputs are complete)
     if ((e = cudaMemcpyAsync(counts, P.totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToDevice, s)) != cudaSuccess)

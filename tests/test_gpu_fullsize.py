@@ -126,3 +126,21 @@ def test_ct_u16_512(pkg, oracle, cuda):
     assert np.array_equal(gf - before_v, of)
     assert np.array_equal(gv[:, 1:], ov[:, 1:])
     assert np.abs(gv[:, 0] - ov[:, 0]).max() <= 1e-12
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_tma_walk_matches_global_load_walk(pkg, cuda, alg, monkeypatch):
+    # with MESHING_GB300_TMA=1 volumes with 16-byte aligned rows are classified
+    # from TMA-staged bricks; the default plain global-load walk must give the
+    # same mesh
+    torch = cuda
+    import meshing_gb300.fields as fields
+    t = fields.gyroid(192, dtype=torch.float32)
+    m = {'mc': pkg.MarchingCubes, 'nsn': pkg.NaiveSurfaceNets}.get(alg, pkg.MarchingTetrahedra)(iso=np.float32(0))
+    v1, f1 = run_device(torch, pkg, t, m, ((0, 1),) * 3)
+    monkeypatch.setenv('MESHING_GB300_TMA', '1')
+    ctx = pkg.Context(0)
+    v2, f2 = run_device(torch, pkg, t, m, ((0, 1),) * 3, ctx=ctx)
+    ctx.close()
+    assert f1.shape[0] > 0
+    assert torch.equal(f1, f2) and torch.equal(v1, v2)
