@@ -7,8 +7,9 @@ seeded a_k ~ N(0,1), |w_k| ~ U[1,8] with a random direction, phi_k ~ U[0,2pi)).
 The volume is 4 GiB, larger than L2, so no flush is needed between steps.
 
 Metric: Gvoxels/s counting input samples nx*ny*nz.
-  value  -- device-resident: mesh_extract_device (classify -> scan -> emit)
-            with the volume and preallocated outputs in HBM;
+  value  -- device-resident: mesh_extract_device (classify -> scan ->
+            compaction of the active cells -> expansion into vertices and
+            faces) with the volume and preallocated outputs in HBM;
   e2e    -- the two-phase drop-in call (mesh_count + mesh_fill) with pinned
             host buffers: upload, extraction and download of the mesh.
 The roofline object reports the dominant kernel's algorithmic bytes over its
@@ -84,9 +85,13 @@ class Clocks:
         self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
         try:
             self.p = subprocess.Popen(['nvidia-smi', '-i', str(index), '--query-gpu=' + self.Q, '--format=csv,noheader',
-                                       '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       '-lms', '50'], stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        # start timing only once sampling runs
+        t0 = time.time()
+        while self.p is not None and time.time() - t0 < 5 and os.path.getsize(self.f.name) == 0:
+            time.sleep(0.01)
 
     def stop(self):
         if self.p is None:
@@ -175,7 +180,7 @@ def run_ours(args, rank, world, dist):
     X = Y = Z = (0, 1)
     ctx = pkg.Context(local)
     stream = torch.cuda.current_stream(dev)
-    ctx.set_stream(stream.cuda_stream)
+    ctx.follow_torch(dev)  # the timing events are recorded on this stream
     p = pkg.make_params(m, X, Y, Z)
     nv, nf = ctypes.c_int64(), ctypes.c_int64()
     pkg._lib.check(lib.mesh_count(ctx.handle, ctypes.c_void_p(vol.data_ptr()), 2, n, n, n, 1, ctypes.byref(p),
@@ -250,14 +255,16 @@ def run_ours(args, rank, world, dist):
     in_b = vox * 4
     out_b = nv * 12 + nf * 24
     stage = {k: v[0] / max(v[1], 1) for k, v in st.items()}
-    # algorithmic bytes per launch: classify reads every sample once (4 B); the emit
-    # stage (active-cell compaction + expansion) writes the mesh (12 B per vertex,
-    # 24 B per face); the scan reads 3 u32 counts and writes 3 int64 bases per piece
-    emit_ms = stage['emit'] + stage['expand']
+    # algorithmic bytes per launch: classify (k_classify) reads every sample once
+    # (4 B); the emit stage -- compaction of the active cells (k_compact_mc, a
+    # second read of the volume) and their expansion (k_expand_mc) -- writes the
+    # mesh (12 B per vertex, 24 B per face); the scan reads 3 u32 counts and
+    # writes 3 int64 bases per piece.  The active-cell list between compaction and
+    # expansion is not counted.
     kern = {
-        'classify': {'ms': stage['classify'], 'bytes': in_b},
-        'scan': {'ms': stage['scan'], 'bytes': float((n - 1) ** 2 * 3 * (4 + 8))},
-        'emit': {'ms': emit_ms, 'bytes': float(out_b), 'launches': ['compact', 'expand'],
+        'classify': {'ms': stage['classify'], 'bytes': in_b, 'kernel': 'k_classify'},
+        'scan': {'ms': stage['scan'], 'bytes': float((n - 1) ** 2 * 3 * (4 + 8)), 'kernel': 'k_scan'},
+        'emit': {'ms': stage['emit'] + stage['expand'], 'bytes': float(out_b), 'kernel': 'k_compact_mc + k_expand_mc',
                  'compact_ms': stage['emit'], 'expand_ms': stage['expand']},
     }
     for k in kern.values():
@@ -306,7 +313,7 @@ def run_ours(args, rank, world, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--steps', type=int, default=100)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--n', type=int, default=N_DEFAULT, help='grid size per axis (default 1024)')

@@ -78,6 +78,9 @@ def check(rc, ctx=None):
         raise MeshError(rc, msg)
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream
+
+
 class Context:
     """Owns a mesh_ctx (device scratch, stream) for one CUDA device."""
 
@@ -104,7 +107,10 @@ class Context:
 
     def stage_times(self):
         """{stage: (total device ms, kernel launches)} since the last query; stages are
-        classify, scan, emit (MC active-cell compaction, or the whole MT/NSN emit), expand."""
+        classify (with MESHING_GB300_ONE_WALK=1, the Marching Cubes walk that also
+        lists the active cells), scan, emit (MC: compaction of the active cells by
+        a second walk; MT/NSN: the whole emit), expand (MC: active cells into
+        vertices and faces)."""
         ms = (ctypes.c_double * 4)()
         n = (ctypes.c_int64 * 4)()
         check(self._lib.mesh_ctx_stage_times(self.handle, ms, n), self.handle)
@@ -114,4 +120,14 @@ class Context:
         check(self._lib.mesh_ctx_sync(self.handle), self.handle)
 
     def set_stream(self, stream_handle):
+        """Issue work on the cudaStream_t `stream_handle`; None = the context's own stream."""
         check(self._lib.mesh_ctx_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)), self.handle)
+
+    def follow_torch(self, device):
+        """Issue work on torch's current stream of `device`.  Torch's default
+        stream has handle 0, which the C ABI reads as "the context's own
+        stream"; it is passed as cudaStreamLegacy instead, so that the work is
+        ordered after the kernels that produced the volume."""
+        import torch
+        h = torch.cuda.current_stream(device).cuda_stream
+        self.set_stream(h if h else CUDA_STREAM_LEGACY)

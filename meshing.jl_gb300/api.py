@@ -183,7 +183,7 @@ def isosurface(A, *args, ctx=None):
             raise TypeError('unsupported volume eltype %s' % A.dtype)
         t = _torch_julia_layout(A)
         c = ctx or default_context(t.device.index or 0)
-        c.set_stream(torch.cuda.current_stream(t.device).cuda_stream)
+        c.follow_torch(t.device)
         nv, nf = ctypes.c_int64(), ctypes.c_int64()
         nx, ny, nz = t.shape
         check(lib.mesh_count(c.handle, ctypes.c_void_p(t.data_ptr()), dt, nx, ny, nz, 1, ctypes.byref(p),
@@ -234,7 +234,7 @@ def isosurface_device(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), verts=Non
     dt = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}[A.dtype]
     t = _torch_julia_layout(A)
     c = ctx or default_context(t.device.index or 0)
-    c.set_stream(torch.cuda.current_stream(t.device).cuda_stream)
+    c.follow_torch(t.device)
     if counts is None:
         counts = torch.zeros(2, dtype=torch.int64, device=t.device)
     nx, ny, nz = t.shape

@@ -1,7 +1,7 @@
-// K3 (Marching Cubes) -- emit vertices and faces at the scanned offsets.
+// K3 (Marching Cubes), two-pass form -- emit vertices and faces at the
+// scanned offsets, after a second walk over the volume.
 //
-// Replaces process_mc_voxel! (src/marching_cubes.jl:67-92), vertex_interp
-// (:100-104) and mc_vert_points (:111-120).  Two kernels:
+// Replaces process_mc_voxel! (src/marching_cubes.jl:67-92).  Two kernels:
 //
 // K3a compact.  Persistent warps walk the classify kernel's tiles (31 x-cells
 // by WY y-cells, one z segment), skipping z chunks whose activity bytes are
@@ -11,24 +11,15 @@
 // reference's emission order.  Every 256th entry also records the global
 // vertex and face offsets of its cell.
 //
-// K3b expand.  Each CTA takes 256 consecutive entries, scans their vertex and
-// face counts, and turns them into one task per output vertex and one per
-// face.  Consecutive threads write consecutive vertices and faces, so the
-// mesh is stored with fully coalesced writes.
+// K3b expand (mesh_mc.cuh, k_expand_mc<..., false>).
 //
-// Arithmetic follows Julia's promotion exactly (no FMA contraction):
-//   mu = (iso - v1) / (v2 - v1)         in Q (UInt16 differences wrap)
-//   p  = p1 + mu * (p2 - p1)             in P = promote(Q, eltype(LinRange))
-// then rounded to the output eltype.  On the two axes an edge does not move
-// along, p2 - p1 == 0 and the result is p1 itself unless p1 == 0 or mu is not
-// finite, in which case the literal expression is evaluated.  When P is
-// Float64 but mu and the output are Float32, the moving coordinate is
-// computed by the exact float path fast_f32_pos and only undecidable cases
-// fall back to FP64.
+// This is the default form: the one walk of k_walk_mc.cu reads the volume
+// once but costs more in total on GB300.  Its scratch is also known exactly
+// after the scan, which the allocation-free entry point needs.
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
-#include "mesh_point.cuh"
+#include "mesh_mc.cuh"
 
 #include <algorithm>
 
@@ -36,127 +27,7 @@ namespace mesh {
 
 namespace {
 
-constexpr unsigned FULL = 0xffffffffu;
 constexpr int U = 2;     // z planes loaded ahead (only active chunks are walked)
-constexpr int XW = 256;  // K3b threads per CTA == entries per block
-static_assert(XW == ENT_BLOCK, "one expansion CTA per block of entries");
-
-// MC edges (src/lut/mc.jl:606-608) on the corner order of src/marching_cubes.jl:111-120,
-// 9 bits per edge: a | b<<3 | moving axis<<6 | negative direction<<8; edges 0-5 in
-// EDGE_LO, 6-11 in EDGE_HI, so the lookup needs no (lane-divergent) branch.
-#define MC_EDGE(a, b, ax, neg) ((unsigned long long)((a) | (b) << 3 | (ax) << 6 | (neg) << 8))
-constexpr unsigned long long EDGE_LO = MC_EDGE(0, 1, 0, 0) | MC_EDGE(1, 2, 1, 0) << 9 | MC_EDGE(2, 3, 0, 1) << 18 |
-                                       MC_EDGE(3, 0, 1, 1) << 27 | MC_EDGE(4, 5, 0, 0) << 36 | MC_EDGE(5, 6, 1, 0) << 45;
-constexpr unsigned long long EDGE_HI = MC_EDGE(6, 7, 0, 1) | MC_EDGE(7, 4, 1, 1) << 9 | MC_EDGE(0, 4, 2, 0) << 18 |
-                                       MC_EDGE(1, 5, 2, 0) << 27 | MC_EDGE(2, 6, 2, 0) << 36 | MC_EDGE(3, 7, 2, 0) << 45;
-#undef MC_EDGE
-__device__ __forceinline__ int edge_info(int e) {
-    const unsigned long long w = e < 6 ? EDGE_LO : EDGE_HI;
-    return (int)((w >> (9 * (e < 6 ? e : e - 6))) & 0x1ffu);
-}
-// corner k of the MC order -> offsets: x 0 1 1 0 0 1 1 0, y 0 0 1 1 0 0 1 1, z 0 0 0 0 1 1 1 1
-__device__ __forceinline__ int cdx(int k) { return ((k + 1) >> 1) & 1; }
-__device__ __forceinline__ int cdy(int k) { return (k >> 1) & 1; }
-__device__ __forceinline__ int cdz(int k) { return (k >> 2) & 1; }
-
-// p1 + mu*d in P, rounded to float: the literal evaluation, kept out of line so
-// that the rare cases that need it do not occupy the FP64 pipe for every vertex.
-template <class P> __device__ __noinline__ float moving_fp64(double c1, double d, double m) {
-    return (float)Ar<P>::add((P)c1, Ar<P>::mul((P)m, (P)d));
-}
-struct F3 {
-    float v[3];
-};
-template <class P> __device__ __noinline__ F3 still_fp64(const Plan *pp, int xa, int ya, int za, double m) {
-    const Plan &p = *pp;
-    F3 o;
-    o.v[0] = (float)Ar<P>::add(tab<P>(p.xp, p.xpf, xa), Ar<P>::mul((P)m, P(0)));
-    o.v[1] = (float)Ar<P>::add(tab<P>(p.yp, p.ypf, ya), Ar<P>::mul((P)m, P(0)));
-    o.v[2] = (float)Ar<P>::add(tab<P>(p.zp, p.zpf, za), Ar<P>::mul((P)m, P(0)));
-    return o;
-}
-
-// The vertex on MC edge e of cell (x, y, z) with corner values va (start) and
-// vbv (end), written to verts[out].
-template <class T, class Q, class P>
-__device__ __forceinline__ void vertex_task(const Plan &p, int e, int x, int y, int z, T va, T vbv, int64_t out) {
-    const int g = edge_info(e);
-    const int a = g & 7, ax = (g >> 6) & 3, neg = (g >> 8) & 1;
-    const int xa = x + cdx(a), ya = y + cdy(a), za = z + cdz(a);
-    const Q mu = quotient<Q>(va, vbv, p);
-    // moving axis: p1 + mu * (+-(p[i+1] - p[i]))
-    const int ia = ax == 0 ? xa : (ax == 1 ? ya : za);
-    const double *tp = ax == 0 ? p.xp : (ax == 1 ? p.yp : p.zp);
-    const double *td = ax == 0 ? p.dx : (ax == 1 ? p.dy : p.dz);
-    const float *tpf = ax == 0 ? p.xpf : (ax == 1 ? p.ypf : p.zpf);
-    const float *tdf = ax == 0 ? p.dxf : (ax == 1 ? p.dyf : p.dzf);
-    const int id = neg ? ia - 1 : ia;
-    const bool fin = isfinite(mu);
-    if (p.out64) {
-        const P m = (P)mu;
-        const P c1 = tab<P>(tp, tpf, ia);
-        const P d = tab<P>(td, tdf, id);
-        const P rm = Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
-        double o0 = __ldg(p.xp + xa), o1 = __ldg(p.yp + ya), o2 = __ldg(p.zp + za);
-        if (!fin || o0 == 0.0 || o1 == 0.0 || o2 == 0.0) {
-            o0 = (double)Ar<P>::add((P)o0, Ar<P>::mul(m, P(0)));
-            o1 = (double)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
-            o2 = (double)Ar<P>::add((P)o2, Ar<P>::mul(m, P(0)));
-        }
-        double *o = (double *)p.verts + 3 * out;
-        o[0] = ax == 0 ? (double)rm : o0;
-        o[1] = ax == 1 ? (double)rm : o1;
-        o[2] = ax == 2 ? (double)rm : o2;
-    } else if (sizeof(P) == 4) {
-        const P m = (P)mu;
-        const P c1 = tab<P>(tp, tpf, ia);
-        const P d = tab<P>(td, tdf, id);
-        const float fr = (float)Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
-        float o0 = __ldg(p.xpf + xa), o1 = __ldg(p.ypf + ya), o2 = __ldg(p.zpf + za);
-        if (!fin || o0 == 0.0f || o1 == 0.0f || o2 == 0.0f) {
-            o0 = (float)Ar<P>::add((P)o0, Ar<P>::mul(m, P(0)));
-            o1 = (float)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
-            o2 = (float)Ar<P>::add((P)o2, Ar<P>::mul(m, P(0)));
-        }
-        float *o = (float *)p.verts + 3 * out;
-        o[0] = ax == 0 ? fr : o0;
-        o[1] = ax == 1 ? fr : o1;
-        o[2] = ax == 2 ? fr : o2;
-    } else {
-        // Float64 positions rounded to Float32 output
-        float fr;
-        bool done = false;
-        if (sizeof(Q) == 4 && !p.force_fp64) {
-            // Float32 mu: exact float fast path
-            const int64_t off = (ax == 0 ? 0 : (ax == 1 ? p.nx : p.nx + p.ny));
-            const float *sp = p.split;
-            const float dh = __ldg(sp + 2 * p.ntab + off + id), dl = __ldg(sp + 3 * p.ntab + off + id);
-            done = fin && fast_f32_pos((float)mu, __ldg(sp + off + ia), __ldg(sp + p.ntab + off + ia),
-                                       neg ? -dh : dh, neg ? -dl : dl, fr);
-        }
-        if (!done) {
-            const double d = __ldg(td + id);
-            fr = moving_fp64<P>(__ldg(tp + ia), neg ? -d : d, (double)mu);
-        }
-        F3 ov = {{__ldg(p.xpf + xa), __ldg(p.ypf + ya), __ldg(p.zpf + za)}};
-        if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f) ov = still_fp64<P>(&p, xa, ya, za, (double)mu);
-        float *o = (float *)p.verts + 3 * out;
-        o[0] = ax == 0 ? fr : ov.v[0];
-        o[1] = ax == 1 ? fr : ov.v[1];
-        o[2] = ax == 2 ? fr : ov.v[2];
-    }
-}
-
-// 8 corner values of an entry, stored contiguously.
-template <class T> __device__ __forceinline__ void store8(T *dst, const T (&v)[8]) {
-#pragma unroll
-    for (int k = 0; k < 8; k++) dst[k] = v[k];
-}
-template <> __device__ __forceinline__ void store8<float>(float *dst, const float (&v)[8]) {
-    float4 *d = reinterpret_cast<float4 *>(dst);
-    d[0] = make_float4(v[0], v[1], v[2], v[3]);
-    d[1] = make_float4(v[4], v[5], v[6], v[7]);
-}
 
 // ---------------------------------------------------------------- K3a ----
 
@@ -297,123 +168,11 @@ __global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems)
     }
 }
 
-// ---------------------------------------------------------------- K3b ----
-
-template <class T> struct ExpandSmem {
-    T val[8][XW];
-    unsigned long long pos[XW];
-    int32_t vs[XW], fs[XW];
-    uint8_t cs[XW];
-    uint8_t vmap[XW * MC_MAX_VERTS];
-    uint8_t fmap[XW * MC_MAX_FACES];
-    int32_t wsum[2][XW / 32];
-};
-
-template <class T, class Q, class P>
-__global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
-    __shared__ uint64_t s_v[256], s_f[256];
-    __shared__ ExpandSmem<T> sm;
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-        s_v[i] = MC_CASE_VERTS[i];
-        s_f[i] = MC_CASE_FACES[i];
-    }
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int64_t na = min(p.totals[2], p.ent_cap);
-    const int64_t nblocks = (na + XW - 1) / XW;
-    const uint64_t pmask = (1ull << POS_BITS) - 1;
-    __syncthreads();
-
-    for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
-        const int64_t e = blk * XW + tid;
-        int nv = 0, nf = 0;
-        if (e < na) {
-            const int cs = p.ent_cs[e];
-            const uint64_t t = s_v[cs];
-            nv = (int)((t >> 48) & 15u);
-            nf = (int)((t >> 52) & 7u);
-            sm.cs[tid] = (uint8_t)cs;
-            sm.pos[tid] = p.ent_pos[e];
-            const T *src = (const T *)p.ent_val + 8 * e;
-#pragma unroll
-            for (int k = 0; k < 8; k++) sm.val[k][tid] = src[k];
-        }
-        // block exclusive scan of (nv, nf)
-        int iv = nv, jf = nf;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int a = __shfl_up_sync(FULL, iv, o), b = __shfl_up_sync(FULL, jf, o);
-            if (lane >= o) {
-                iv += a;
-                jf += b;
-            }
-        }
-        if (lane == 31) {
-            sm.wsum[0][w] = iv;
-            sm.wsum[1][w] = jf;
-        }
-        __syncthreads();
-        int wv = 0, wf = 0, V = 0, F = 0;
-#pragma unroll
-        for (int k = 0; k < XW / 32; k++) {
-            const int a = sm.wsum[0][k], b = sm.wsum[1][k];
-            if (k < w) {
-                wv += a;
-                wf += b;
-            }
-            V += a;
-            F += b;
-        }
-        const int vs = wv + iv - nv, fs = wf + jf - nf;
-        sm.vs[tid] = vs;
-        sm.fs[tid] = fs;
-        for (int k = 0; k < nv; k++) sm.vmap[vs + k] = (uint8_t)tid;
-        for (int k = 0; k < nf; k++) sm.fmap[fs + k] = (uint8_t)tid;
-        const int64_t vb0 = nblocks ? p.ent_side[2 * blk] : 0, fb0 = nblocks ? p.ent_side[2 * blk + 1] : 0;
-        __syncthreads();
-        if ((unsigned long long)(vb0 + V) > (unsigned long long)p.verts_cap ||
-            (unsigned long long)(fb0 + F) > (unsigned long long)p.faces_cap) {
-            if (tid == 0) atomicOr(p.err, ERR_CAPACITY);
-        } else {
-            for (int t = tid; t < V; t += XW) {
-                const int j = sm.vmap[t];
-                const int k = t - sm.vs[j];
-                const uint64_t pos = sm.pos[j];
-                const int ed = (int)((s_v[sm.cs[j]] >> (4 * k)) & 15u);
-                const int g = edge_info(ed);
-                vertex_task<T, Q, P>(p, ed, (int)(pos & pmask), (int)((pos >> POS_BITS) & pmask),
-                                     (int)(pos >> (2 * POS_BITS)), sm.val[g & 7][j], sm.val[(g >> 3) & 7][j], vb0 + t);
-            }
-            for (int t = tid; t < F; t += XW) {
-                const int j = sm.fmap[t];
-                const int k = t - sm.fs[j];
-                const unsigned s = (unsigned)(s_f[sm.cs[j]] >> (12 * k));
-                const int64_t vb = vb0 + sm.vs[j];
-                int64_t *o = p.faces + 3 * (fb0 + t);
-                o[0] = vb + (s & 15u) + 1;
-                o[1] = vb + ((s >> 4) & 15u) + 1;
-                o[2] = vb + ((s >> 8) & 15u) + 1;
-            }
-        }
-        __syncthreads();
-    }
-}
-
-int resident_ctas(const void *fn, int threads) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1) {
-        cudaGetLastError();
-        per_sm = 1;
-    }
-    return per_sm * sms;
-}
-
 template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cudaStream_t s) {
     static int grid_a = 0, grid_b = 0;  // per instantiation: resident CTAs on this device
     if (!grid_a) {
         grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
-        grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P>, XW);
+        grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P, false>, XW);
     }
     if (stage == 0) {
         const int nitems = p.tiles_x * p.tiles_y * p.nseg;
@@ -421,7 +180,7 @@ template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cu
         if (e != cudaSuccess) return e;
         k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);
     } else {
-        k_expand_mc<T, Q, P><<<grid_b, XW, 0, s>>>(p);
+        k_expand_mc<T, Q, P, false><<<grid_b, XW, 0, s>>>(p);
     }
     return cudaGetLastError();
 }

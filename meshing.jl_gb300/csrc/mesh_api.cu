@@ -35,7 +35,10 @@ using namespace mesh;
 
 namespace {
 
-constexpr int NSTAGE = 4;  // classify, scan, emit (walk), expand
+constexpr int NSTAGE = 4;  // classify (or the one-walk MC pass), scan, emit (second walk), expand
+// device word slots of the misc buffer: totals[NCNT], error word, work counter,
+// staging counter
+constexpr int MISC_SLOTS = NCNT + 3;
 
 struct DevBuf {
     void *ptr = nullptr;
@@ -76,6 +79,7 @@ struct mesh_ctx {
     int have_plan = 0;
     int Q64 = 0, A64 = 0, P64 = 0;
     int64_t nverts = 0, nfaces = 0, nactive = 0;
+    int64_t ent_cap_seen = 0;  // largest active-cell list prepared on this context
     std::string msg;
     // stage timing (diagnostics)
     int timing = 0;
@@ -83,6 +87,12 @@ struct mesh_ctx {
     // MESHING_GB300_TMA=1: classify from TMA-staged bricks.  Off by default: on
     // GB300 the plain global-load walk is faster (1.24 vs 1.29 ms at 1024^3 f32).
     int want_tma = 0;
+    // MESHING_GB300_ONE_WALK=1: Marching Cubes in one walk that also lists the
+    // active cells (k_walk_mc.cu).  Off by default: on GB300 the walk is issue
+    // bound, so dropping the second read of the volume saves little, and
+    // expanding the cells in walk order scatters the output writes (1024^3 f32:
+    // walk 2.24 + expand 1.41 ms vs classify 1.24 + compact 1.18 + expand 0.75 ms).
+    int one_walk = 0;
     int use_tma = 0;     // the current plan streams the volume through TMA
     CUtensorMap tmap;
     std::vector<cudaEvent_t> ev_free;
@@ -314,10 +324,12 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     P.flags = (uint8_t *)c->flags.ptr;
     P.scan_state = (unsigned long long *)c->scan.ptr;
     P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + (size_t)st * NCNT * sizeof(unsigned long long));
-    // misc: totals[NCNT] int64, then the error word and the work counter
+    // misc: totals[NCNT] int64, then the error word, the work counter and the
+    // staging counter
     P.totals = (int64_t *)c->misc.ptr;
     P.err = (unsigned int *)((int64_t *)c->misc.ptr + NCNT);
     P.work = (unsigned int *)((int64_t *)c->misc.ptr + NCNT + 1);
+    P.stage_next = (unsigned long long *)((int64_t *)c->misc.ptr + NCNT + 2);
     P.scan_spin_limit = 1 << 24;
     return MESH_OK;
 }
@@ -385,14 +397,18 @@ bool make_tensor_map(mesh_ctx *c) {
            CUDA_SUCCESS;
 }
 
+// Marching Cubes walked once, classification staging the active cells (opt-in).
+bool one_walk(const mesh_ctx *c) { return c->plan.alg == MESH_ALG_MC && c->one_walk; }
+
 int run_count(mesh_ctx *c) {
     Plan &P = c->plan;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(c->misc.ptr, 0, (NCNT + 2) * sizeof(int64_t), c->stream)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(c->misc.ptr, 0, MISC_SLOTS * sizeof(int64_t), c->stream)) != cudaSuccess)
         return cuda_fail(c, e, "memset");
-    c->use_tma = make_tensor_map(c);
+    c->use_tma = !one_walk(c) && make_tensor_map(c);
     mark(c, 0);
-    e = c->use_tma ? launch_classify_tma(P, c->tmap, c->stream) : launch_classify(P, c->stream);
+    if (one_walk(c)) e = launch_walk_mc(P, c->stream);
+    else e = c->use_tma ? launch_classify_tma(P, c->tmap, c->stream) : launch_classify(P, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "classify launch");
     mark(c, 0);
     mark(c, 1);
@@ -406,12 +422,12 @@ int check_err(mesh_ctx *c) {
     if (err & ERR_SCAN_TIMEOUT) return fail(c, MESH_EDEVICE, "scan look-back wait expired");
     if (err & ERR_TMA_TIMEOUT) return fail(c, MESH_EDEVICE, "TMA stage wait expired");
     if (err & ERR_BOUNDS) return fail(c, MESH_EDEVICE, "device bounds check failed");
-    if (err & ERR_CAPACITY) return fail(c, MESH_ECAPACITY, "output capacity too small");
+    if (err & (ERR_CAPACITY | ERR_STAGE)) return fail(c, MESH_ECAPACITY, "output capacity too small");
     return MESH_OK;
 }
 
 int fetch_misc(mesh_ctx *c) {
-    cudaError_t e = cudaMemcpyAsync(c->h_misc, c->misc.ptr, (NCNT + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+    cudaError_t e = cudaMemcpyAsync(c->h_misc, c->misc.ptr, MISC_SLOTS * sizeof(int64_t), cudaMemcpyDeviceToHost,
                                     c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "synchronize");
@@ -419,7 +435,7 @@ int fetch_misc(mesh_ctx *c) {
     return MESH_OK;
 }
 
-// Compact list of active cells (Marching Cubes), room for `cap` entries.
+// List of active cells (Marching Cubes), room for `cap` entries.
 int ensure_entries(mesh_ctx *c, int64_t cap) {
     Plan &P = c->plan;
     const size_t es = P.T == MESH_DT_U16 ? 2 : P.T == MESH_DT_F32 ? 4 : 8;
@@ -427,7 +443,8 @@ int ensure_entries(mesh_ctx *c, int64_t cap) {
     auto up = [](size_t n) { return (n + 255) / 256 * 256; };  // every array 256-byte aligned
     const size_t o_val = up((size_t)cap * 8);
     const size_t o_side = o_val + up((size_t)cap * 8 * es);
-    const size_t o_cs = o_side + up((size_t)nside * 16);
+    const size_t o_rank = o_side + up((size_t)nside * 16);
+    const size_t o_cs = o_rank + up((size_t)cap * 8);
     const size_t bytes = o_cs + up((size_t)cap + 1);
     cudaError_t e = c->ent.ensure(bytes);
     if (e != cudaSuccess) return cuda_fail(c, e, "entry buffer");
@@ -435,13 +452,21 @@ int ensure_entries(mesh_ctx *c, int64_t cap) {
     P.ent_pos = (unsigned long long *)b;
     P.ent_val = b + o_val;  // 8 corner values per entry (vector stores need 16-byte alignment)
     P.ent_side = (long long *)(b + o_side);
+    P.ent_rank = (uint2 *)(b + o_rank);
     P.ent_cs = (uint8_t *)(b + o_cs);
     P.ent_cap = cap;
+    c->ent_cap_seen = std::max(c->ent_cap_seen, cap);
     return MESH_OK;
 }
 
 int launch_emit(mesh_ctx *c) {
     cudaError_t e;
+    if (one_walk(c)) {
+        mark(c, 3);
+        e = launch_expand_staged_mc(c->plan, c->Q64, c->P64, c->stream);
+        mark(c, 3);
+        return e != cudaSuccess ? cuda_fail(c, e, "expand launch") : MESH_OK;
+    }
     mark(c, 2);
     if (c->plan.alg == MESH_ALG_MC) e = launch_emit_mc(c->plan, c->Q64, c->P64, 0, c->stream);
     else e = launch_emit_halo(c->plan, c->Q64, c->A64, c->P64, c->stream);
@@ -455,6 +480,9 @@ int launch_emit(mesh_ctx *c) {
     }
     return MESH_OK;
 }
+
+// Staging slots of the one walk beyond its active cells: at most a block per warp.
+int64_t stage_slack(const Plan &P) { return (int64_t)STG_BLK * P.tiles_x * P.tiles_y * P.nseg; }
 
 bool degenerate(int64_t nx, int64_t ny, int64_t nz) { return nx < 2 || ny < 2 || nz < 2; }
 
@@ -507,8 +535,8 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     c->device = device;
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess ||
-        c->misc.ensure(64) != cudaSuccess ||
-        cudaHostAlloc((void **)&c->h_misc, (NCNT + 2) * sizeof(int64_t), cudaHostAllocDefault) != cudaSuccess) {
+        c->misc.ensure(MISC_SLOTS * sizeof(int64_t)) != cudaSuccess ||
+        cudaHostAlloc((void **)&c->h_misc, MISC_SLOTS * sizeof(int64_t), cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         mesh_ctx_destroy(c);
         return MESH_ENOMEM;
@@ -518,6 +546,8 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     c->force_fp64 = ff && ff[0] == '1';
     const char *wt = getenv("MESHING_GB300_TMA");
     c->want_tma = wt && wt[0] == '1';
+    const char *ow = getenv("MESHING_GB300_ONE_WALK");
+    c->one_walk = ow && ow[0] == '1';
     *out = c;
     return MESH_OK;
 }
@@ -569,8 +599,21 @@ int mesh_count(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int6
     }
     if (!vol) return fail(c, MESH_EINVAL, "volume is NULL");
     if ((rc = prepare(c, vol, T, nx, ny, nz, vol_on_device, p))) return rc;
+    if (one_walk(c)) {
+        // the list of active cells is filled during the count: start from a
+        // guess (or the context's earlier list), and if the walk ran out of
+        // slots walk again with the exact number it reported
+        const int64_t cells = (int64_t)c->plan.cx * c->plan.cy * c->plan.cz;
+        const int64_t guess = std::max<int64_t>(c->ent_cap_seen, cells / 48 + stage_slack(c->plan));
+        if ((rc = ensure_entries(c, guess))) return rc;
+    }
     if ((rc = run_count(c))) return rc;
     if ((rc = fetch_misc(c))) return rc;
+    if (one_walk(c) && ((unsigned)c->h_misc[NCNT] & ERR_STAGE)) {
+        if ((rc = ensure_entries(c, c->h_misc[NCNT + 2]))) return rc;
+        if ((rc = run_count(c))) return rc;
+        if ((rc = fetch_misc(c))) return rc;
+    }
     if ((rc = check_err(c))) return rc;
     c->nverts = c->h_misc[0];
     c->nfaces = c->h_misc[1];
@@ -602,7 +645,7 @@ int mesh_fill(mesh_ctx *c, void *verts, int64_t *faces, int out_on_device) {
     P.verts_cap = c->nverts;
     P.faces_cap = c->nfaces;
     int rc;
-    if (P.alg == MESH_ALG_MC && (rc = ensure_entries(c, c->nactive))) return rc;
+    if (P.alg == MESH_ALG_MC && !one_walk(c) && (rc = ensure_entries(c, c->nactive))) return rc;
     if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
     if ((rc = launch_emit(c))) return rc;
     if (!out_on_device) {
@@ -637,8 +680,11 @@ int mesh_extract_device(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t
     P.faces = faces;
     P.verts_cap = verts ? verts_cap : 0;
     P.faces_cap = faces ? faces_cap : 0;
-    // an active Marching Cubes cell emits at least 3 vertices
-    if (P.alg == MESH_ALG_MC && (rc = ensure_entries(c, P.verts_cap / 3))) return rc;
+    // an active Marching Cubes cell emits at least 3 vertices; the one walk
+    // also leaves up to a block of slots per warp unused
+    if (P.alg == MESH_ALG_MC &&
+        (rc = ensure_entries(c, P.verts_cap / 3 + (one_walk(c) ? stage_slack(P) : 0))))
+        return rc;
     if ((rc = run_count(c))) return rc;
     if ((rc = launch_emit(c))) return rc;
     if ((e = cudaMemcpyAsync(counts, P.totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream)) !=

@@ -25,6 +25,7 @@ constexpr int POS_BITS = 21;     // bits per coordinate in a packed cell positio
 constexpr unsigned ERR_SCAN_TIMEOUT = 1u;
 constexpr unsigned ERR_CAPACITY = 2u;
 constexpr unsigned ERR_BOUNDS = 4u;
+constexpr unsigned ERR_STAGE = 16u;  // the staged entry list was too short (8 is the TMA wait)
 
 struct Plan {
     // volume (Julia layout: x fastest)
@@ -68,13 +69,17 @@ struct Plan {
     int64_t *totals;      // [NCNT] total vertices, faces, active cells
     unsigned int *err;    // device error word
     unsigned int *work;   // work-item counter of the persistent kernels
-    // compact list of active cells in emission order (Marching Cubes):
-    // packed x | y << 21 | z << 42, case, the 8 corner values, and for every
-    // 256th entry the vertex / face offsets of that entry
+    // list of active cells (Marching Cubes): packed x | y << 21 | z << 42,
+    // case, the 8 corner values; in emission order with, for every 256th
+    // entry, the vertex / face offsets of that entry (ent_side), or in the
+    // order the walk found them with each entry's vertex / face rank inside
+    // its piece (ent_rank) and *stage_next slots handed out
     unsigned long long *ent_pos;
     uint8_t *ent_cs;
     void *ent_val;
     long long *ent_side;
+    uint2 *ent_rank;
+    unsigned long long *stage_next;
     int64_t ent_cap;
     // outputs
     void *verts;
@@ -92,6 +97,10 @@ inline __host__ __device__ int64_t piece(const Plan &p, int seg, int y, int x) {
 cudaError_t launch_classify(const Plan &p, cudaStream_t s);
 cudaError_t launch_scan(const Plan &p, cudaStream_t s);
 cudaError_t launch_emit(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
+// Marching Cubes in one walk: classify + stage entries, then expand them.
+constexpr int STG_BLK = 128;  // staging slots a walking warp takes at a time
+cudaError_t launch_walk_mc(const Plan &p, cudaStream_t s);
+cudaError_t launch_expand_staged_mc(const Plan &p, int Q64, int P64, cudaStream_t s);
 
 }  // namespace mesh
 

@@ -87,3 +87,36 @@ def test_range_arguments(pkg):
     assert list(p.range) == [-2, 2, 0, 1, -1, 1] and p.range_type == 4
     p = pkg.make_params(pkg.MarchingCubes(), np.array([0.0, 0.5, 1.0]), (np.float64(-1), 1.0), (0.0, 2.0))
     assert list(p.range) == [0, 1, -1, 1, 0, 2] and p.range_type == 3
+
+
+def test_torch_default_stream_is_passed_as_the_legacy_stream(pkg, monkeypatch):
+    # torch's default stream has handle 0, which mesh_ctx_set_stream reads as
+    # "the context's own (non-blocking) stream"; work on a torch volume must be
+    # ordered after the kernels that wrote it, so the binding passes
+    # cudaStreamLegacy (1) instead, and other streams unchanged
+    import torch
+    from meshing_gb300 import _lib
+
+    seen = []
+
+    class FakeLib:
+        def mesh_ctx_set_stream(self, h, s):
+            seen.append(s.value)
+            return 0
+
+        def mesh_ctx_destroy(self, h):
+            pass
+
+    class FakeStream:
+        def __init__(self, h):
+            self.cuda_stream = h
+
+    c = _lib.Context.__new__(_lib.Context)
+    c._lib, c.handle, c.device = FakeLib(), ctypes.c_void_p(1234), 0
+    for h, want in [(0, 1), (0xabc000, 0xabc000)]:
+        monkeypatch.setattr(torch.cuda, 'current_stream', lambda device=None, h=h: FakeStream(h))
+        c.follow_torch(0)
+        assert seen[-1] == want
+    c.set_stream(None)
+    assert seen[-1] is None  # NULL: the context's own stream
+    c.handle = None
