@@ -148,6 +148,44 @@ MESH_API int mesh_extract_noalloc(const void *vol, int vol_dtype, int64_t nx, in
                                   const mesh_params *p, void *verts, int64_t verts_cap, int64_t *faces,
                                   int64_t faces_cap, int64_t *counts, void *stream);
 
+/* ---- Batches: Marching Cubes over many device volumes in one pass ----------
+ * No counterpart in the reference, which extracts one volume per call
+ * (src/marching_cubes.jl:27-64); each volume of a batch gives exactly what
+ * that call gives on it alone.  The stages run once over a flattened worklist
+ * of all volumes' tiles, with one scan across the batch, instead of one launch
+ * sequence per volume.  Work is queued on the context's stream. */
+typedef struct mesh_batch mesh_batch;
+/* n volumes of dtype `vol_dtype` in device memory (Julia layout), vols[i] with
+ * sizes dims[3i..3i+2], extracted with the MarchingCubes parameters p
+ * (p->alg must be MESH_ALG_MC).  ranges: n x 6 endpoints (x0 x1 y0 y1 z0 z1,
+ * of p->range_type), or NULL for p->range on every volume.  Pointers and sizes
+ * are fixed for the batch's lifetime; the volumes' contents may change. */
+MESH_API int mesh_batch_create(mesh_ctx *ctx, int n, const void *const *vols, int vol_dtype, const int64_t *dims,
+                               const mesh_params *p, const double *ranges, mesh_batch **out);
+MESH_API void mesh_batch_destroy(mesh_batch *b);
+/* Classifies and scans every volume (waits for the result) and sizes the
+ * batch's outputs exactly: total vertices and faces. */
+MESH_API int mesh_batch_count(mesh_batch *b, int64_t *nverts, int64_t *nfaces);
+/* Queues the whole extraction into the batch's outputs; with graphs enabled it
+ * is captured once into a CUDA graph and replayed.  Outputs larger than at the
+ * last count are reported by mesh_batch_sync as MESH_ECAPACITY. */
+MESH_API int mesh_batch_run(mesh_batch *b);
+/* Waits for the batch's work and reports device-side errors. */
+MESH_API int mesh_batch_sync(mesh_batch *b);
+/* Device pointers of the outputs: vertices [V][3] of float(FT), faces [F][3]
+ * int64, 1-based within each volume, and offsets [n+1][2]: the first vertex
+ * and first face of volume i (row n holds the totals). */
+MESH_API int mesh_batch_outputs(mesh_batch *b, void **verts, int64_t **faces, int64_t **offsets);
+MESH_API int mesh_batch_set_graph(mesh_batch *b, int enable);
+/* knobs[4]: z cells per work item (0 = whole columns; rounded up to 8),
+ * classify and compact CTAs per SM (0 = as many as fit), threads per scan CTA
+ * (96..1024, a multiple of 32).  A new first knob needs a new count. */
+MESH_API int mesh_batch_set_knobs(mesh_batch *b, const int *knobs);
+MESH_API int mesh_batch_knobs(const mesh_batch *b, int *knobs);
+/* Autotuner: times `reps` runs of every candidate of one knob at a time,
+ * keeps the fastest, counts again; a text report goes to report[report_len]. */
+MESH_API int mesh_batch_tune(mesh_batch *b, int reps, char *report, int report_len);
+
 #ifdef __cplusplus
 }
 #endif

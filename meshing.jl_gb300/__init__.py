@@ -16,7 +16,8 @@ on the GPU through the C ABI (include/meshing_gb300.h); there is no CPU path.
 from ._lib import Context, MeshError, MeshParams, load as load_library
 from .api import (MarchingCubes, MarchingTetrahedra, NaiveSurfaceNets, AbstractMeshingAlgorithm, isosurface,
                   isosurface_device, output_float_bits, make_params, default_context)
+from .batch import Batch
 
 __all__ = ['isosurface', 'isosurface_device', 'MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets',
            'AbstractMeshingAlgorithm', 'MeshError', 'Context', 'MeshParams', 'output_float_bits', 'make_params',
-           'default_context', 'load_library']
+           'default_context', 'load_library', 'Batch']

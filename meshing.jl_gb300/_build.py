@@ -15,8 +15,8 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(BUILD, 'libmeshing_gb300.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-SOURCES = ['mesh_api.cu', 'k_classify.cu', 'k_scan.cu', 'k_walk_mc.cu', 'k_emit_mc.cu', 'k_emit_halo.cu',
-           'mesh_noalloc.cu']
+SOURCES = ['mesh_api.cu', 'k_tables.cu', 'k_classify.cu', 'k_scan.cu', 'k_walk_mc.cu', 'k_emit_mc.cu',
+           'k_emit_halo.cu', 'mesh_noalloc.cu', 'mesh_batch.cu']
 
 
 def nvcc():

@@ -17,7 +17,9 @@ STATUS = {0: 'MESH_OK', 1: 'MESH_EINVAL', 2: 'MESH_ENOMEM', 3: 'MESH_ECUDA', 4: 
 # every symbol the header declares
 EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_ctx_set_stream', 'mesh_status_string',
            'mesh_ctx_last_error', 'mesh_output_float_bits', 'mesh_count', 'mesh_fill', 'mesh_extract_device',
-           'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times', 'mesh_extract_noalloc')
+           'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times', 'mesh_extract_noalloc',
+           'mesh_batch_create', 'mesh_batch_destroy', 'mesh_batch_count', 'mesh_batch_run', 'mesh_batch_sync',
+           'mesh_batch_outputs', 'mesh_batch_set_graph', 'mesh_batch_set_knobs', 'mesh_batch_knobs', 'mesh_batch_tune')
 
 
 class MeshParams(ctypes.Structure):
@@ -60,6 +62,16 @@ def load():
         'mesh_ctx_enable_timing': (c_int, [vp, c_int]),
         'mesh_ctx_stage_times': (c_int, [vp, P(ctypes.c_double), P(i64)]),
         'mesh_extract_noalloc': (c_int, [vp, c_int, i64, i64, i64, P(MeshParams), vp, i64, vp, i64, vp, vp]),
+        'mesh_batch_create': (c_int, [vp, c_int, P(vp), c_int, P(i64), P(MeshParams), P(ctypes.c_double), P(vp)]),
+        'mesh_batch_destroy': (None, [vp]),
+        'mesh_batch_count': (c_int, [vp, P(i64), P(i64)]),
+        'mesh_batch_run': (c_int, [vp]),
+        'mesh_batch_sync': (c_int, [vp]),
+        'mesh_batch_outputs': (c_int, [vp, P(vp), P(vp), P(vp)]),
+        'mesh_batch_set_graph': (c_int, [vp, c_int]),
+        'mesh_batch_set_knobs': (c_int, [vp, P(c_int)]),
+        'mesh_batch_knobs': (c_int, [vp, P(c_int)]),
+        'mesh_batch_tune': (c_int, [vp, c_int, ctypes.c_char_p, c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -16,6 +16,8 @@
 #include "mesh_tables.h"
 #include "mesh_tma.cuh"
 
+#include <algorithm>
+
 namespace mesh {
 
 namespace {
@@ -118,7 +120,7 @@ __device__ __forceinline__ void chunk_end(const Plan &p, int lane, int tx, int y
 
 __device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, int y0, int seg, const Counts &c) {
     if (!cellx) return;
-    const int64_t np = npieces(p);
+    const int64_t np = p.pstride;
 #pragma unroll
     for (int r = 0; r < WY; r++) {
         if (y0 + r < p.cy) {
@@ -130,18 +132,10 @@ __device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, 
     }
 }
 
-// Walk with one coalesced global load per lane, row and plane (any layout).
+// Walk of warp tile (tx, ty) through z segment seg with one coalesced global
+// load per lane, row and plane (any layout).
 template <class T, int ALG>
-__global__ void __launch_bounds__(256) k_classify(const Plan p) {
-    __shared__ uint32_t s_tab[256];
-    load_tables<ALG>(s_tab);
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31;
-    const int ty = blockIdx.y * WARPS + (threadIdx.x >> 5);
-    if (ty >= p.tiles_y) return;  // warp-uniform
-    const int tx = blockIdx.x;
-    const int seg = blockIdx.z;
+__device__ __forceinline__ void classify_tile(const Plan &p, const uint32_t *s_tab, int lane, int tx, int ty, int seg) {
     const int xs = tx * TILE_X + lane;
     const int y0 = ty * WY;
     const int zbeg = seg * p.zs;
@@ -199,6 +193,39 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
         }
     }
     store_counts(p, cellx, xs, y0, seg, c);
+}
+
+template <class T, int ALG>
+__global__ void __launch_bounds__(256) k_classify(const Plan p) {
+    __shared__ uint32_t s_tab[256];
+    load_tables<ALG>(s_tab);
+    __syncthreads();
+    const int ty = blockIdx.y * WARPS + (threadIdx.x >> 5);
+    if (ty >= p.tiles_y) return;  // warp-uniform
+    classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
+}
+
+// Batch (Marching Cubes): persistent warps take work items -- a warp tile of
+// one volume's z segment, volumes in order, y tiles fastest -- from a counter.
+template <class T>
+__global__ void __launch_bounds__(256) k_classify_batch(const Plan p) {
+    __shared__ uint32_t s_tab[256];
+    load_tables<MESH_ALG_MC>(s_tab);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned item = 0;
+        if (lane == 0) item = atomicAdd(p.work, 1u);
+        item = __shfl_sync(FULL, item, 0);
+        if ((int64_t)item >= p.nitems) break;
+        const BatchVol b = p.bvols[p.item_vol[item]];
+        const Plan pv = vol_view(p, b);
+        const int64_t local = (int64_t)item - b.item0;
+        const int ty = (int)(local % b.tiles_y);
+        const int tx = (int)((local / b.tiles_y) % b.tiles_x);
+        const int seg = (int)(local / ((int64_t)b.tiles_y * b.tiles_x));
+        classify_tile<T, MESH_ALG_MC>(pv, s_tab, lane, tx, ty, seg);
+    }
 }
 
 // Walk over TMA-staged bricks.  The CTA's 31 x 32 cells of a z segment are
@@ -357,6 +384,34 @@ cudaError_t launch_classify_tma(const Plan &p, const CUtensorMap &map, cudaStrea
     case MESH_DT_F32: return launch_tma_t<float>(p, map, s);
     default: return launch_tma_t<double>(p, map, s);
     }
+}
+
+int persistent_grid(const void *fn, int threads, int ctas_per_sm) {
+    int dev = 0, sms = 0, fit = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, threads, 0) != cudaSuccess || fit < 1) {
+        cudaGetLastError();
+        fit = 1;
+    }
+    return sms * (ctas_per_sm > 0 ? std::min(ctas_per_sm, fit) : fit);
+}
+
+cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s) {
+    const void *fn = nullptr;
+    switch (p.T) {
+    case MESH_DT_U16: fn = (const void *)k_classify_batch<uint16_t>; break;
+    case MESH_DT_F32: fn = (const void *)k_classify_batch<float>; break;
+    default: fn = (const void *)k_classify_batch<double>; break;
+    }
+    const int grid = (int)std::min<int64_t>(persistent_grid(fn, 32 * WARPS, ctas), (p.nitems + WARPS - 1) / WARPS);
+    if (grid < 1) return cudaSuccess;
+    switch (p.T) {
+    case MESH_DT_U16: k_classify_batch<uint16_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    case MESH_DT_F32: k_classify_batch<float><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    default: k_classify_batch<double><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_classify(const Plan &p, cudaStream_t s) {

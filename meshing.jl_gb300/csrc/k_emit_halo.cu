@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
     const bool realx = cellx && lane >= 1;
     const T *vol = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
-    const int64_t np = npieces(p);
+    const int64_t np = p.pstride;
 
     bool rowok[R + 1];
     const T *rowp[R + 1];

@@ -11,7 +11,7 @@
 // reference's emission order.  Every 256th entry also records the global
 // vertex and face offsets of its cell.
 //
-// K3b expand (mesh_mc.cuh, k_expand_mc<..., false>).
+// K3b expand (mesh_mc.cuh, k_expand_mc<..., EXP_ORDERED>).
 //
 // This is the default form: the one walk of k_walk_mc.cu reads the volume
 // once but costs more in total on GB300.  Its scratch is also known exactly
@@ -31,26 +31,15 @@ constexpr int U = 2;     // z planes loaded ahead (only active chunks are walked
 
 // ---------------------------------------------------------------- K3a ----
 
+// Entries of warp tile (tx, ty) of z segment seg; with a batch, each entry
+// also records its volume `vol`.
 template <class T>
-__global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems) {
-    __shared__ uint64_t s_v[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31;
-    const T *vol = (const T *)p.vol;
+__device__ __forceinline__ void compact_tile(const Plan &p, const uint64_t *s_v, int lane, int tx, int ty, int seg,
+                                             uint32_t vol) {
+    const T *volp = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
-    const int64_t np = npieces(p);
-
-    // persistent warps: take (y tile, x tile, segment) items in order from a counter
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = (int)atomicAdd(p.work, 1u);
-        item = __shfl_sync(FULL, item, 0);
-        if (item >= nitems) break;
-        const int ty = item % p.tiles_y;
-        const int tx = (item / p.tiles_y) % p.tiles_x;
-        const int seg = item / (p.tiles_y * p.tiles_x);
+    const int64_t np = p.pstride;
+    {
         const int xs = tx * TILE_X + lane;
         const int y0 = ty * WY;
         const int zbeg = seg * p.zs;
@@ -62,7 +51,7 @@ __global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems)
 #pragma unroll
         for (int r = 0; r <= WY; r++) {
             rowok[r] = xs < p.nx && y0 + r < p.ny;
-            rowp[r] = rowok[r] ? vol + xs + p.nx * (int64_t)(y0 + r) : vol;
+            rowp[r] = rowok[r] ? volp + xs + p.nx * (int64_t)(y0 + r) : volp;
         }
         const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
         const uint32_t cellm = __ballot_sync(FULL, cellx);
@@ -144,6 +133,7 @@ __global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems)
                                     p.ent_cs[e] = (uint8_t)cm;
                                     const T cv[8] = {a0, a1, b1, b0, c0, c1, d1, d0};
                                     store8<T>((T *)p.ent_val + 8 * e, cv);
+                                    if (p.ent_vol) p.ent_vol[e] = vol;
                                     if ((e & (ENT_BLOCK - 1)) == 0) {
                                         p.ent_side[2 * (e / ENT_BLOCK)] = bv[r];
                                         p.ent_side[2 * (e / ENT_BLOCK) + 1] = bf[r];
@@ -168,11 +158,52 @@ __global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems)
     }
 }
 
+template <class T>
+__global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems) {
+    __shared__ uint64_t s_v[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    // persistent warps: take (y tile, x tile, segment) items in order from a counter
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(p.work, 1u);
+        item = __shfl_sync(FULL, item, 0);
+        if (item >= nitems) break;
+        const int ty = item % p.tiles_y;
+        const int tx = (item / p.tiles_y) % p.tiles_x;
+        const int seg = item / (p.tiles_y * p.tiles_x);
+        compact_tile<T>(p, s_v, lane, tx, ty, seg, 0);
+    }
+}
+
+// Batch: the work items of k_classify_batch, in the same order.
+template <class T>
+__global__ void __launch_bounds__(256, 3) k_compact_batch(const Plan p) {
+    __shared__ uint64_t s_v[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned item = 0;
+        if (lane == 0) item = atomicAdd(p.work, 1u);
+        item = __shfl_sync(FULL, item, 0);
+        if ((int64_t)item >= p.nitems) break;
+        const uint32_t v = p.item_vol[item];
+        const BatchVol b = p.bvols[v];
+        const int64_t local = (int64_t)item - b.item0;
+        const int ty = (int)(local % b.tiles_y);
+        const int tx = (int)((local / b.tiles_y) % b.tiles_x);
+        const int seg = (int)(local / ((int64_t)b.tiles_y * b.tiles_x));
+        compact_tile<T>(vol_view(p, b), s_v, lane, tx, ty, seg, v);
+    }
+}
+
 template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cudaStream_t s) {
     static int grid_a = 0, grid_b = 0;  // per instantiation: resident CTAs on this device
     if (!grid_a) {
         grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
-        grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P, false>, XW);
+        grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>, XW);
     }
     if (stage == 0) {
         const int nitems = p.tiles_x * p.tiles_y * p.nseg;
@@ -180,7 +211,7 @@ template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cu
         if (e != cudaSuccess) return e;
         k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);
     } else {
-        k_expand_mc<T, Q, P, false><<<grid_b, XW, 0, s>>>(p);
+        k_expand_mc<T, Q, P, EXP_ORDERED><<<grid_b, XW, 0, s>>>(p);
     }
     return cudaGetLastError();
 }
@@ -191,7 +222,56 @@ template <class T> cudaError_t go_t(const Plan &p, int Q64, int P64, int stage, 
     return go<T, float, float>(p, stage, s);
 }
 
+int persistent_ctas(const void *fn, int threads, int ctas_per_sm) {
+    int dev = 0, sms = 0, fit = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, threads, 0) != cudaSuccess || fit < 1) {
+        cudaGetLastError();
+        fit = 1;
+    }
+    return sms * (ctas_per_sm > 0 ? std::min(ctas_per_sm, fit) : fit);
+}
+
+template <class T> cudaError_t compact_batch_t(const Plan &p, int ctas, cudaStream_t s) {
+    const int grid = (int)std::min<int64_t>(persistent_ctas((const void *)k_compact_batch<T>, 32 * WARPS, ctas),
+                                            (p.nitems + WARPS - 1) / WARPS);
+    cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess || grid < 1) return e;
+    k_compact_batch<T><<<grid, 32 * WARPS, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <class T, class Q, class P> cudaError_t expand_batch_t(const Plan &p, cudaStream_t s) {
+    static int grid = 0;  // per instantiation: resident CTAs on this device
+    if (!grid) grid = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_BATCH>, XW);
+    k_expand_mc<T, Q, P, EXP_BATCH><<<grid, XW, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <class T> cudaError_t expand_batch_tt(const Plan &p, int Q64, int P64, cudaStream_t s) {
+    if (Q64) return expand_batch_t<T, double, double>(p, s);
+    if (P64) return expand_batch_t<T, float, double>(p, s);
+    return expand_batch_t<T, float, float>(p, s);
+}
+
 }  // namespace
+
+cudaError_t launch_compact_batch(const Plan &p, int ctas, cudaStream_t s) {
+    switch (p.T) {
+    case MESH_DT_U16: return compact_batch_t<uint16_t>(p, ctas, s);
+    case MESH_DT_F32: return compact_batch_t<float>(p, ctas, s);
+    default: return compact_batch_t<double>(p, ctas, s);
+    }
+}
+
+cudaError_t launch_expand_batch(const Plan &p, int Q64, int P64, cudaStream_t s) {
+    switch (p.T) {
+    case MESH_DT_U16: return expand_batch_tt<uint16_t>(p, Q64, P64, s);
+    case MESH_DT_F32: return expand_batch_tt<float>(p, Q64, P64, s);
+    default: return expand_batch_t<double, double, double>(p, s);
+    }
+}
 
 // stage 0: K3a compact (active-cell list); stage 1: K3b expand (vertices and faces)
 cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStream_t s) {

@@ -65,20 +65,18 @@ __device__ int64_t look_back(unsigned long long *state, int tile, int64_t agg, i
     return excl;
 }
 
-__global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
-    __shared__ int s_tile;
-    __shared__ int64_t s_part[NCNT][32][33];
-    __shared__ int64_t s_xpre[NCNT][32];
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.scan_ticket, 1u);
-    __syncthreads();
-    const int tile = s_tile;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int x = tile * 32 + lane;
+// Scan tile `xt` of the (view) plan p -- columns 32*xt .. 32*xt+31 -- which is
+// tile `gt` of `ntiles` in the look-back chain.  The CTA's nw warps split the
+// (y, seg) sequence of every column.
+__device__ __forceinline__ void scan_body(const Plan &p, int xt, int gt, int ntiles, int64_t (*s_part)[32][33],
+                                          int64_t (*s_xpre)[32]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int x = xt * 32 + lane;
     const bool xok = x < p.cx;
     const int64_t L = (int64_t)p.cy * p.nseg;
-    const int64_t per = (L + 31) / 32;
+    const int64_t per = (L + nw - 1) / nw;
     const int64_t j0 = min(L, (int64_t)w * per), j1 = min(L, j0 + per);
-    const int64_t np = npieces(p);
+    const int64_t np = p.pstride;
 
     int64_t sum[NCNT];
 #pragma unroll
@@ -99,7 +97,7 @@ __global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
     if (w < NCNT) {  // warp c scans counter c
         const int c = w;
         int64_t tot = 0;  // column total; s_part becomes the per-warp exclusive prefix
-        for (int k = 0; k < 32; k++) {
+        for (int k = 0; k < nw; k++) {
             const int64_t a = s_part[c][k][lane];
             s_part[c][k][lane] = tot;
             tot += a;
@@ -113,8 +111,8 @@ __global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
         const int64_t agg = __shfl_sync(FULL, inc, 31);
         int64_t pre = 0;
         if (lane == 0) {
-            pre = look_back(p.scan_state + (int64_t)c * ntiles, tile, agg, p.scan_spin_limit, p.err);
-            if (tile == ntiles - 1) p.totals[c] = pre + agg;
+            pre = look_back(p.scan_state + (int64_t)c * ntiles, gt, agg, p.scan_spin_limit, p.err);
+            if (gt == ntiles - 1) p.totals[c] = pre + agg;
         }
         pre = __shfl_sync(FULL, pre, 0);
         s_xpre[c][lane] = pre + inc - tot;
@@ -138,9 +136,62 @@ __global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
     }
 }
 
+__global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
+    __shared__ int s_tile;
+    __shared__ int64_t s_part[NCNT][32][33];
+    __shared__ int64_t s_xpre[NCNT][32];
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.scan_ticket, 1u);
+    __syncthreads();
+    scan_body(p, s_tile, s_tile, ntiles, s_part, s_xpre);
+}
+
+// Batch: the scan tiles of all volumes, volumes in order, form one look-back
+// chain, so every piece gets its offset in the batch's concatenated output and
+// a volume's first piece gives the volume's first vertex and face.
+__global__ void __launch_bounds__(1024) k_scan_batch(const Plan p) {
+    __shared__ int s_tile;
+    __shared__ int64_t s_part[NCNT][32][33];
+    __shared__ int64_t s_xpre[NCNT][32];
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.scan_ticket, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    const BatchVol b = p.bvols[p.stile_vol[t]];
+    scan_body(vol_view(p, b), t - b.stile0, t, p.nstiles, s_part, s_xpre);
+}
+
+// First vertex / face of every volume: the scanned offset of its first piece
+// in emission order (x = y = seg = 0).  A volume without cells shares the
+// offset of the next piece, or the totals.
+__global__ void k_batch_offsets(const Plan p) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v > p.nvols) return;
+    int64_t ov = p.totals[0], of = p.totals[1];
+    if (v < p.nvols) {
+        const int64_t i = p.bvols[v].piece0;
+        if (i < p.pstride) {
+            ov = p.base[i];
+            of = p.base[p.pstride + i];
+        }
+    }
+    p.vol_off[2 * v] = ov;
+    p.vol_off[2 * v + 1] = of;
+}
+
 }  // namespace
 
 int scan_tiles(const Plan &p) { return (p.cx + 31) / 32; }
+
+cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * NCNT * (size_t)p.nstiles, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(p.scan_ticket, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    // no cells at all: the totals stay zero (cleared by the caller)
+    if (p.nstiles > 0) k_scan_batch<<<p.nstiles, threads, 0, s>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_batch_offsets<<<(p.nvols + 1 + 255) / 256, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_scan(const Plan &p, cudaStream_t s) {
     const int ntiles = scan_tiles(p);

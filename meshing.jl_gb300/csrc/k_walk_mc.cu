@@ -15,7 +15,7 @@
 // may continue into the next block, and the unused end of the warp's last
 // block gets case 0.  The per-piece totals go to the scan as from K1.
 //
-// After the scan, k_expand_mc<..., true> (mesh_mc.cuh) writes each entry's
+// After the scan, k_expand_mc<..., EXP_STAGED> (mesh_mc.cuh) writes each entry's
 // vertices and faces at base(piece) + rank.  The volume is read once; the
 // list holds only the ~2% active cells.
 //
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(256, 3) k_walk_mc(const Plan p) {
     if (__any_sync(FULL, over) && lane == 0) atomicOr(p.err, ERR_STAGE);
 
     if (cellx) {
-        const int64_t np = npieces(p);
+        const int64_t np = p.pstride;
 #pragma unroll
         for (int r = 0; r < WY; r++) {
             if (y0 + r < p.cy) {
@@ -205,8 +205,8 @@ template <class T> cudaError_t walk_t(const Plan &p, cudaStream_t s) {
 
 template <class T, class Q, class P> cudaError_t expand_t(const Plan &p, cudaStream_t s) {
     static int grid = 0;  // per instantiation: resident CTAs on this device
-    if (!grid) grid = resident_ctas((const void *)k_expand_mc<T, Q, P, true>, XW);
-    k_expand_mc<T, Q, P, true><<<grid, XW, 0, s>>>(p);
+    if (!grid) grid = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_STAGED>, XW);
+    k_expand_mc<T, Q, P, EXP_STAGED><<<grid, XW, 0, s>>>(p);
     return cudaGetLastError();
 }
 

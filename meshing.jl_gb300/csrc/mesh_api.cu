@@ -3,10 +3,10 @@
 // Turns a reference call isosurface(A, alg, X, Y, Z) into a launch plan:
 // Julia's type promotion (src/marching_cubes.jl:31, src/marching_tetrahedra.jl:131)
 // picks the arithmetic and output types, the LinRange node coordinates
-// (src/marching_cubes.jl:36-38) are tabulated once per call on the host with
-// the exact Base.lerpi arithmetic, and the three kernels run on the context's
-// stream: classify -> scan -> emit.  Device scratch grows monotonically and is
-// reused across calls.
+// (src/marching_cubes.jl:36-38) are tabulated on the device with the exact
+// Base.lerpi arithmetic (k_tables.cu), and the kernels run on the context's
+// stream: classify -> scan -> emit.  Nothing waits on the host between
+// launches.  Device scratch grows monotonically and is reused across calls.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "mesh_host.h"
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
 #include "mesh_tma.cuh"
@@ -33,73 +34,7 @@ int scan_tiles(const Plan &p);
 
 using namespace mesh;
 
-namespace {
-
-constexpr int NSTAGE = 4;  // classify (or the one-walk MC pass), scan, emit (second walk), expand
-// device word slots of the misc buffer: totals[NCNT], error word, work counter,
-// staging counter
-constexpr int MISC_SLOTS = NCNT + 3;
-
-struct DevBuf {
-    void *ptr = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t n) {
-        if (n <= cap) return cudaSuccess;
-        size_t want = std::max(n, cap + cap / 4);
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&ptr, want);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            e = cudaMalloc(&ptr, n);
-            if (e != cudaSuccess) return e;
-            want = n;
-        }
-        cap = want;
-        return cudaSuccess;
-    }
-    void release() {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        cap = 0;
-    }
-};
-
-}  // namespace
-
-struct mesh_ctx {
-    int device = 0;
-    int sms = 148;
-    cudaStream_t own = nullptr;
-    cudaStream_t stream = nullptr;
-    DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f, ent;
-    int64_t *h_misc = nullptr;  // pinned: totals[NCNT], err
-    Plan plan{};
-    int have_plan = 0;
-    int Q64 = 0, A64 = 0, P64 = 0;
-    int64_t nverts = 0, nfaces = 0, nactive = 0;
-    int64_t ent_cap_seen = 0;  // largest active-cell list prepared on this context
-    std::string msg;
-    // stage timing (diagnostics)
-    int timing = 0;
-    int force_fp64 = 0;  // MESHING_GB300_FORCE_FP64=1: evaluate every Float64 position in FP64
-    // MESHING_GB300_TMA=1: classify from TMA-staged bricks.  Off by default: on
-    // GB300 the plain global-load walk is faster (1.24 vs 1.29 ms at 1024^3 f32).
-    int want_tma = 0;
-    // MESHING_GB300_ONE_WALK=1: Marching Cubes in one walk that also lists the
-    // active cells (k_walk_mc.cu).  Off by default: on GB300 the walk is issue
-    // bound, so dropping the second read of the volume saves little, and
-    // expanding the cells in walk order scatters the output writes (1024^3 f32:
-    // walk 2.24 + expand 1.41 ms vs classify 1.24 + compact 1.18 + expand 0.75 ms).
-    int one_walk = 0;
-    int use_tma = 0;     // the current plan streams the volume through TMA
-    CUtensorMap tmap;
-    std::vector<cudaEvent_t> ev_free;
-    std::vector<cudaEvent_t> ev_pairs[NSTAGE];  // start, stop, start, stop, ...
-};
-
-namespace {
+namespace mesh {
 
 constexpr double EXACT_INT = 9007199254740992.0;  // 2^53
 
@@ -170,17 +105,6 @@ int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_
     return MESH_OK;
 }
 
-// LinRange(a, b, n) in eltype L (Base.lerpi): T((1-t)*a + t*b), t = i/(n-1).
-void linrange(int L32, double a, double b, int64_t n, double *out) {
-    const double aa = L32 ? (double)(float)a : a, bb = L32 ? (double)(float)b : b;
-    const int64_t d = n > 1 ? n - 1 : 1;
-    for (int64_t i = 0; i < n; i++) {
-        const double t = (double)i / (double)d;
-        const double v = (1.0 - t) * aa + t * bb;
-        out[i] = L32 ? (double)(float)v : v;
-    }
-}
-
 void own_masks(uint32_t own[8]) {
     for (int bnd = 0; bnd < 8; bnd++) {
         uint32_t m = 0;
@@ -195,22 +119,16 @@ void own_masks(uint32_t own[8]) {
     }
 }
 
-int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
-            const mesh_params *p) {
-    Plan &P = c->plan;
-    P = Plan{};
-    c->have_plan = 0;
-    P.nx = nx; P.ny = ny; P.nz = nz;
-    P.cx = (int32_t)(nx - 1); P.cy = (int32_t)(ny - 1); P.cz = (int32_t)(nz - 1);
+void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P64) {
     P.T = T;
     P.alg = p->alg;
     const int I = p->iso_type, E = p->eps_type, Rt = p->range_type;
     const int mt = p->alg == MESH_ALG_MT;
-    c->Q64 = T == MESH_DT_F64 || I == MESH_DT_F64 || (T == MESH_DT_U16 && I == MESH_DT_I64);
+    *Q64 = T == MESH_DT_F64 || I == MESH_DT_F64 || (T == MESH_DT_U16 && I == MESH_DT_I64);
     const int L32 = Rt == MESH_DT_F32;
-    c->A64 = mt ? (c->Q64 || E == MESH_DT_F64) : c->Q64;
-    c->P64 = c->A64 || !L32;
-    if (!mt) c->P64 = c->Q64 || !L32;
+    *A64 = mt ? (*Q64 || E == MESH_DT_F64) : *Q64;
+    *P64 = *A64 || !L32;
+    if (!mt) *P64 = *Q64 || !L32;
     const int tys[4] = {Rt, T, I, E};
     P.out64 = out_is_f64(tys, mt ? 4 : 3);
 
@@ -236,6 +154,21 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
         P.hi_f = (float)hi;
         own_masks(P.own);
     }
+}
+
+}  // namespace mesh
+
+namespace {
+
+int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
+            const mesh_params *p) {
+    Plan &P = c->plan;
+    P = Plan{};
+    c->have_plan = 0;
+    P.nx = nx; P.ny = ny; P.nz = nz;
+    P.cx = (int32_t)(nx - 1); P.cy = (int32_t)(ny - 1); P.cz = (int32_t)(nz - 1);
+    set_types(P, T, p, &c->Q64, &c->A64, &c->P64);
+    const int L32 = p->range_type == MESH_DT_F32;
 
     // tiling
     P.tiles_x = (P.cx + TILE_X - 1) / TILE_X;
@@ -266,52 +199,17 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     }
 
     // coordinate tables: xp yp zp dx dy dz (double), the same as float, then the
-    // hi/lo float split of the nodes and spacings
+    // hi/lo float split of the nodes and spacings, computed on the device
     const int64_t ntab = nx + ny + nz;
-    const size_t tbytes = (size_t)ntab * 2 * (sizeof(double) + sizeof(float)) + (size_t)ntab * 4 * sizeof(float);
-    double *h = (double *)malloc(tbytes);
-    if (!h) return fail(c, MESH_ENOMEM, "host table buffer");
-    double *hp = h, *hd = h + ntab;
-    float *hpf = (float *)(h + 2 * ntab), *hdf = hpf + ntab;
-    float *hs = hdf + ntab;  // p_hi, p_lo, d_hi, d_lo
-    const int64_t ns[3] = {nx, ny, nz};
-    int64_t off = 0;
-    for (int a = 0; a < 3; a++) {
-        linrange(L32, p->range[2 * a], p->range[2 * a + 1], ns[a], hp + off);
-        for (int64_t i = 0; i < ns[a]; i++) {
-            double d = 0;
-            if (i + 1 < ns[a]) {
-                d = hp[off + i + 1] - hp[off + i];
-                if (L32) d = (double)((float)hp[off + i + 1] - (float)hp[off + i]);
-            }
-            const double v = hp[off + i];
-            hd[off + i] = d;
-            hpf[off + i] = (float)v;
-            hdf[off + i] = (float)d;
-            hs[off + i] = (float)v;
-            hs[ntab + off + i] = (float)(v - (double)(float)v);
-            hs[2 * ntab + off + i] = (float)d;
-            hs[3 * ntab + off + i] = (float)(d - (double)(float)d);
-        }
-        off += ns[a];
-    }
-    if ((e = c->tabs.ensure(tbytes)) != cudaSuccess) { free(h); return cuda_fail(c, e, "table buffer"); }
-    e = cudaMemcpyAsync(c->tabs.ptr, h, tbytes, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // h is pageable and freed below
-    free(h);
-    if (e != cudaSuccess) return cuda_fail(c, e, "table upload");
-    double *dp = (double *)c->tabs.ptr;
-    P.xp = dp; P.yp = dp + nx; P.zp = dp + nx + ny;
-    P.dx = dp + ntab; P.dy = P.dx + nx; P.dz = P.dx + nx + ny;
-    float *fp = (float *)(dp + 2 * ntab);
-    P.xpf = fp; P.ypf = fp + nx; P.zpf = fp + nx + ny;
-    P.dxf = fp + ntab; P.dyf = P.dxf + nx; P.dzf = P.dxf + nx + ny;
-    P.split = fp + 2 * ntab;
-    P.ntab = ntab;
+    if ((e = c->tabs.ensure(table_bytes(ntab))) != cudaSuccess) return cuda_fail(c, e, "table buffer");
+    if ((e = launch_tables((double *)c->tabs.ptr, nx, ny, nz, p->range, L32, c->stream)) != cudaSuccess)
+        return cuda_fail(c, e, "table launch");
+    bind_tables(P, (double *)c->tabs.ptr, nx, ny, nz);
     P.force_fp64 = c->force_fp64;
 
     // scratch
     const int64_t np = npieces(P);
+    P.pstride = np;
     if ((e = c->cnt.ensure((size_t)np * NCNT * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(c, e, "count buffer");
     if ((e = c->base.ensure((size_t)np * NCNT * sizeof(int64_t))) != cudaSuccess) return cuda_fail(c, e, "base buffer");
     const size_t fb = (size_t)P.nchunks * P.tiles_x * P.cy;

@@ -1,0 +1,90 @@
+// Host-side state shared by the single-volume runtime (mesh_api.cu) and the
+// batched runtime (mesh_batch.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "mesh_internal.cuh"
+
+namespace mesh {
+
+constexpr int NSTAGE = 4;  // classify (or the one-walk MC pass), scan, emit (second walk), expand
+// device word slots of the misc buffer: totals[NCNT], error word, work counter,
+// staging counter
+constexpr int MISC_SLOTS = NCNT + 3;
+
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        size_t want = std::max(n, cap + cap / 4);
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            e = cudaMalloc(&ptr, n);
+            if (e != cudaSuccess) return e;
+            want = n;
+        }
+        cap = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct mesh_ctx {
+    int device = 0;
+    int sms = 148;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    mesh::DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f, ent;
+    int64_t *h_misc = nullptr;  // pinned: totals[NCNT], err
+    mesh::Plan plan{};
+    int have_plan = 0;
+    int Q64 = 0, A64 = 0, P64 = 0;
+    int64_t nverts = 0, nfaces = 0, nactive = 0;
+    int64_t ent_cap_seen = 0;  // largest active-cell list prepared on this context
+    std::string msg;
+    // stage timing (diagnostics)
+    int timing = 0;
+    int force_fp64 = 0;  // MESHING_GB300_FORCE_FP64=1: evaluate every Float64 position in FP64
+    // MESHING_GB300_TMA=1: classify from TMA-staged bricks.  Off by default: on
+    // GB300 the plain global-load walk is faster (1.24 vs 1.29 ms at 1024^3 f32).
+    int want_tma = 0;
+    // MESHING_GB300_ONE_WALK=1: Marching Cubes in one walk that also lists the
+    // active cells (k_walk_mc.cu).  Off by default: on GB300 the walk is issue
+    // bound, so dropping the second read of the volume saves little, and
+    // expanding the cells in walk order scatters the output writes (1024^3 f32:
+    // walk 2.24 + expand 1.41 ms vs classify 1.24 + compact 1.18 + expand 0.75 ms).
+    int one_walk = 0;
+    int use_tma = 0;     // the current plan streams the volume through TMA
+    CUtensorMap tmap;
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<cudaEvent_t> ev_pairs[mesh::NSTAGE];  // start, stop, start, stop, ...
+};
+
+namespace mesh {
+
+// Error helpers: record a message on the context and return the status.
+int fail(mesh_ctx *c, int status, const char *fmt, ...);
+int cuda_fail(mesh_ctx *c, cudaError_t e, const char *what);
+// Argument checks shared by every entry point.
+int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_params *p);
+// Julia's promotion: arithmetic types (Q64: quotient in Float64, A64: MT clamp in
+// Float64, P64: positions in Float64), output eltype and the exact thresholds.
+void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P64);
+
+}  // namespace mesh

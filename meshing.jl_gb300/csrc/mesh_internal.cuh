@@ -27,6 +27,8 @@ constexpr unsigned ERR_CAPACITY = 2u;
 constexpr unsigned ERR_BOUNDS = 4u;
 constexpr unsigned ERR_STAGE = 16u;  // the staged entry list was too short (8 is the TMA wait)
 
+struct BatchVol;
+
 struct Plan {
     // volume (Julia layout: x fastest)
     const void *vol;
@@ -61,6 +63,7 @@ struct Plan {
     int32_t zs, nseg, chunks_per_seg, nchunks;
     int32_t tiles_x, tiles_y;  // classify tiling (TILE_X x WY cells)
     // scratch
+    int64_t pstride;      // elements between the counters' arrays in cnt / base
     uint32_t *cnt;        // [NCNT][nseg][cy][cx] per-piece vertex / face / active-cell counts
     int64_t *base;        // [NCNT][nseg][cy][cx] exclusive prefix in traversal order
     uint8_t *flags;       // [nchunks][tiles_x][cy] 1 if the tile row has an active cell
@@ -86,14 +89,99 @@ struct Plan {
     int64_t *faces;
     int64_t verts_cap, faces_cap;
     int32_t scan_spin_limit;
+    // batches (Marching Cubes over many volumes in one pass): per-volume
+    // descriptors, the volume of each work item and of each scan tile, the
+    // volume of each active-cell entry, and the first vertex / face of every
+    // volume ([nvols + 1][2], the last row the totals)
+    const BatchVol *bvols;
+    const uint32_t *item_vol, *stile_vol;
+    uint32_t *ent_vol;
+    int64_t *vol_off;
+    int64_t nitems;
+    int32_t nvols, nstiles;
+};
+
+// One volume of a batch.  Its work items, pieces, activity bytes and scan
+// tiles are ranges of the batch's arrays starting at item0, piece0, flag0 and
+// stile0; its coordinate tables are a block at `tabs` (k_tables.cu layout).
+struct BatchVol {
+    const void *vol;
+    const double *tabs;
+    int64_t nx, ny, nz;
+    int32_t cx, cy, cz, tiles_x, tiles_y, nseg, zs, chunks_per_seg, nchunks, stile0;
+    int64_t item0, piece0, flag0;
 };
 
 inline __host__ __device__ int64_t npieces(const Plan &p) { return (int64_t)p.nseg * p.cy * p.cx; }
+
+// Coordinate tables of one volume (pointers into its table block).
+struct Tabs {
+    const double *xp, *yp, *zp, *dx, *dy, *dz;
+    const float *xpf, *ypf, *zpf, *dxf, *dyf, *dzf, *split;
+    int64_t ntab, nx, ny;
+};
+inline __host__ __device__ Tabs tabs_of(const Plan &p) {
+    return Tabs{p.xp, p.yp, p.zp, p.dx, p.dy, p.dz, p.xpf, p.ypf, p.zpf, p.dxf, p.dyf, p.dzf, p.split,
+                p.ntab, p.nx, p.ny};
+}
+// The tables of a block at dp (k_tables.cu layout) for nx, ny, nz nodes.
+inline __host__ __device__ Tabs tabs_at(const double *dp, int64_t nx, int64_t ny, int64_t nz) {
+    const int64_t ntab = nx + ny + nz;
+    const double *dd = dp + ntab;
+    const float *fp = (const float *)(dp + 2 * ntab), *fd = fp + ntab;
+    return Tabs{dp, dp + nx, dp + nx + ny, dd, dd + nx, dd + nx + ny, fp, fp + nx, fp + nx + ny,
+                fd, fd + nx, fd + nx + ny, fp + 2 * ntab, ntab, nx, ny};
+}
+inline __host__ __device__ void set_tabs(Plan &P, const Tabs &t) {
+    P.xp = t.xp; P.yp = t.yp; P.zp = t.zp; P.dx = t.dx; P.dy = t.dy; P.dz = t.dz;
+    P.xpf = t.xpf; P.ypf = t.ypf; P.zpf = t.zpf; P.dxf = t.dxf; P.dyf = t.dyf; P.dzf = t.dzf;
+    P.split = t.split;
+    P.ntab = t.ntab;
+}
+// The batch plan p seen as a plan of its volume b alone (shared arrays offset).
+inline __host__ __device__ Plan vol_view(const Plan &p, const BatchVol &b) {
+    Plan v = p;
+    v.vol = b.vol;
+    v.nx = b.nx; v.ny = b.ny; v.nz = b.nz;
+    v.cx = b.cx; v.cy = b.cy; v.cz = b.cz;
+    v.tiles_x = b.tiles_x; v.tiles_y = b.tiles_y;
+    v.nseg = b.nseg; v.zs = b.zs; v.chunks_per_seg = b.chunks_per_seg; v.nchunks = b.nchunks;
+    v.cnt = p.cnt + b.piece0;
+    v.base = p.base + b.piece0;
+    v.flags = p.flags + b.flag0;
+    set_tabs(v, tabs_at(b.tabs, b.nx, b.ny, b.nz));
+    return v;
+}
 inline __host__ __device__ int64_t piece(const Plan &p, int seg, int y, int x) {
     return ((int64_t)seg * p.cy + y) * p.cx + x;
 }
 
+// Coordinate tables (k_tables.cu): bytes for ntab = nx+ny+nz nodes, and the
+// Plan's pointers into a table block at dp.
+inline size_t table_bytes(int64_t ntab) {
+    return (size_t)ntab * 2 * (sizeof(double) + sizeof(float)) + (size_t)ntab * 4 * sizeof(float);
+}
+inline void bind_tables(Plan &P, const double *dp, int64_t nx, int64_t ny, int64_t nz) {
+    set_tabs(P, tabs_at(dp, nx, ny, nz));
+}
+
 // Launchers (each returns cudaError_t of the launch).
+cudaError_t launch_tables(double *tabs, int64_t nx, int64_t ny, int64_t nz, const double *range, int L32,
+                          cudaStream_t s);
+// Tables of many volumes: job i fills the block at dst[i] (one CTA row per job).
+struct TabJob {
+    double *dst;
+    int64_t nx, ny, nz;
+    double range[6];
+};
+cudaError_t launch_tables_batch(const TabJob *jobs, int njobs, int64_t max_ntab, int L32, cudaStream_t s);
+// Batched Marching Cubes stages (k_classify.cu, k_scan.cu, k_emit_mc.cu);
+// ctas: CTAs per SM of the persistent kernels (0 = as many as fit), threads:
+// threads per scan CTA.
+cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s);
+cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s);
+cudaError_t launch_compact_batch(const Plan &p, int ctas, cudaStream_t s);
+cudaError_t launch_expand_batch(const Plan &p, int Q64, int P64, cudaStream_t s);
 cudaError_t launch_classify(const Plan &p, cudaStream_t s);
 cudaError_t launch_scan(const Plan &p, cudaStream_t s);
 cudaError_t launch_emit(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);

@@ -55,29 +55,30 @@ template <class P> __device__ __noinline__ float moving_fp64(double c1, double d
 struct F3 {
     float v[3];
 };
-template <class P> __device__ __noinline__ F3 still_fp64(const Plan *pp, int xa, int ya, int za, double m) {
-    const Plan &p = *pp;
+template <class P> __device__ __noinline__ F3 still_fp64(const Tabs *tp, int xa, int ya, int za, double m) {
+    const Tabs &t = *tp;
     F3 o;
-    o.v[0] = (float)Ar<P>::add(tab<P>(p.xp, p.xpf, xa), Ar<P>::mul((P)m, P(0)));
-    o.v[1] = (float)Ar<P>::add(tab<P>(p.yp, p.ypf, ya), Ar<P>::mul((P)m, P(0)));
-    o.v[2] = (float)Ar<P>::add(tab<P>(p.zp, p.zpf, za), Ar<P>::mul((P)m, P(0)));
+    o.v[0] = (float)Ar<P>::add(tab<P>(t.xp, t.xpf, xa), Ar<P>::mul((P)m, P(0)));
+    o.v[1] = (float)Ar<P>::add(tab<P>(t.yp, t.ypf, ya), Ar<P>::mul((P)m, P(0)));
+    o.v[2] = (float)Ar<P>::add(tab<P>(t.zp, t.zpf, za), Ar<P>::mul((P)m, P(0)));
     return o;
 }
 
 // The vertex on MC edge e of cell (x, y, z) with corner values va (start) and
-// vbv (end), written to verts[out].
+// vbv (end), written to verts[out]; node coordinates from the volume's tables tb.
 template <class T, class Q, class P>
-__device__ __forceinline__ void vertex_task(const Plan &p, int e, int x, int y, int z, T va, T vbv, int64_t out) {
+__device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e, int x, int y, int z, T va, T vbv,
+                                            int64_t out) {
     const int g = edge_info(e);
     const int a = g & 7, ax = (g >> 6) & 3, neg = (g >> 8) & 1;
     const int xa = x + cdx(a), ya = y + cdy(a), za = z + cdz(a);
     const Q mu = quotient<Q>(va, vbv, p);
     // moving axis: p1 + mu * (+-(p[i+1] - p[i]))
     const int ia = ax == 0 ? xa : (ax == 1 ? ya : za);
-    const double *tp = ax == 0 ? p.xp : (ax == 1 ? p.yp : p.zp);
-    const double *td = ax == 0 ? p.dx : (ax == 1 ? p.dy : p.dz);
-    const float *tpf = ax == 0 ? p.xpf : (ax == 1 ? p.ypf : p.zpf);
-    const float *tdf = ax == 0 ? p.dxf : (ax == 1 ? p.dyf : p.dzf);
+    const double *tp = ax == 0 ? tb.xp : (ax == 1 ? tb.yp : tb.zp);
+    const double *td = ax == 0 ? tb.dx : (ax == 1 ? tb.dy : tb.dz);
+    const float *tpf = ax == 0 ? tb.xpf : (ax == 1 ? tb.ypf : tb.zpf);
+    const float *tdf = ax == 0 ? tb.dxf : (ax == 1 ? tb.dyf : tb.dzf);
     const int id = neg ? ia - 1 : ia;
     const bool fin = isfinite(mu);
     if (p.out64) {
@@ -85,7 +86,7 @@ __device__ __forceinline__ void vertex_task(const Plan &p, int e, int x, int y, 
         const P c1 = tab<P>(tp, tpf, ia);
         const P d = tab<P>(td, tdf, id);
         const P rm = Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
-        double o0 = __ldg(p.xp + xa), o1 = __ldg(p.yp + ya), o2 = __ldg(p.zp + za);
+        double o0 = __ldg(tb.xp + xa), o1 = __ldg(tb.yp + ya), o2 = __ldg(tb.zp + za);
         if (!fin || o0 == 0.0 || o1 == 0.0 || o2 == 0.0) {
             o0 = (double)Ar<P>::add((P)o0, Ar<P>::mul(m, P(0)));
             o1 = (double)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
@@ -100,7 +101,7 @@ __device__ __forceinline__ void vertex_task(const Plan &p, int e, int x, int y, 
         const P c1 = tab<P>(tp, tpf, ia);
         const P d = tab<P>(td, tdf, id);
         const float fr = (float)Ar<P>::add(c1, Ar<P>::mul(m, neg ? -d : d));
-        float o0 = __ldg(p.xpf + xa), o1 = __ldg(p.ypf + ya), o2 = __ldg(p.zpf + za);
+        float o0 = __ldg(tb.xpf + xa), o1 = __ldg(tb.ypf + ya), o2 = __ldg(tb.zpf + za);
         if (!fin || o0 == 0.0f || o1 == 0.0f || o2 == 0.0f) {
             o0 = (float)Ar<P>::add((P)o0, Ar<P>::mul(m, P(0)));
             o1 = (float)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
@@ -116,18 +117,18 @@ __device__ __forceinline__ void vertex_task(const Plan &p, int e, int x, int y, 
         bool done = false;
         if (sizeof(Q) == 4 && !p.force_fp64) {
             // Float32 mu: exact float fast path
-            const int64_t off = (ax == 0 ? 0 : (ax == 1 ? p.nx : p.nx + p.ny));
-            const float *sp = p.split;
-            const float dh = __ldg(sp + 2 * p.ntab + off + id), dl = __ldg(sp + 3 * p.ntab + off + id);
-            done = fin && fast_f32_pos((float)mu, __ldg(sp + off + ia), __ldg(sp + p.ntab + off + ia),
+            const int64_t off = (ax == 0 ? 0 : (ax == 1 ? tb.nx : tb.nx + tb.ny));
+            const float *sp = tb.split;
+            const float dh = __ldg(sp + 2 * tb.ntab + off + id), dl = __ldg(sp + 3 * tb.ntab + off + id);
+            done = fin && fast_f32_pos((float)mu, __ldg(sp + off + ia), __ldg(sp + tb.ntab + off + ia),
                                        neg ? -dh : dh, neg ? -dl : dl, fr);
         }
         if (!done) {
             const double d = __ldg(td + id);
             fr = moving_fp64<P>(__ldg(tp + ia), neg ? -d : d, (double)mu);
         }
-        F3 ov = {{__ldg(p.xpf + xa), __ldg(p.ypf + ya), __ldg(p.zpf + za)}};
-        if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f) ov = still_fp64<P>(&p, xa, ya, za, (double)mu);
+        F3 ov = {{__ldg(tb.xpf + xa), __ldg(tb.ypf + ya), __ldg(tb.zpf + za)}};
+        if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f) ov = still_fp64<P>(&tb, xa, ya, za, (double)mu);
         float *o = (float *)p.verts + 3 * out;
         o[0] = ax == 0 ? fr : ov.v[0];
         o[1] = ax == 1 ? fr : ov.v[1];
@@ -153,17 +154,24 @@ template <> __device__ __forceinline__ void store8<float>(float *dst, const floa
 // consecutive threads write consecutive outputs of an entry and of
 // neighbouring entries.
 //
-// STAGED = false: entries are in emission order (k_compact_mc); every 256th
+// EXP_ORDERED: entries are in emission order (k_compact_mc); every 256th
 // entry carries the global vertex / face offsets of its cell (ent_side), the
 // others follow by the block scan.  Entries: totals[2].
-// STAGED = true: entries are in the order the walk found them (k_walk_mc);
-// each carries its vertex / face rank inside its piece (ent_rank), and the
-// scanned piece offsets give the global ones.  Entries: *stage_next slots,
-// of which unused ones have case 0 and emit nothing.
+// EXP_STAGED: entries are in the order the walk found them (k_walk_mc); each
+// carries its vertex / face rank inside its piece (ent_rank), and the scanned
+// piece offsets give the global ones.  Entries: *stage_next slots, of which
+// unused ones have case 0 and emit nothing.
+// EXP_BATCH: as EXP_ORDERED over the volumes of a batch in order
+// (k_compact_batch); each entry also names its volume (ent_vol), whose
+// coordinate tables place its vertices and whose first vertex makes its faces
+// 1-based within the volume.
+
+constexpr int EXP_ORDERED = 0, EXP_STAGED = 1, EXP_BATCH = 2;
 
 template <class T> struct ExpandSmem {
     T val[8][XW];
     unsigned long long pos[XW];
+    uint32_t vol[XW];  // EXP_BATCH: the entry's volume
     long long vb[XW], fb[XW];  // global offsets of each entry's first vertex / face
     int32_t vs[XW], fs[XW];    // block-local offsets
     uint8_t cs[XW];
@@ -172,8 +180,15 @@ template <class T> struct ExpandSmem {
     int32_t wsum[2][XW / 32];
 };
 
-template <class T, class Q, class P, bool STAGED>
+// Coordinate tables of batch volume v.
+__device__ __forceinline__ Tabs batch_tabs(const Plan &p, uint32_t v) {
+    const BatchVol &b = p.bvols[v];
+    return tabs_at(b.tabs, b.nx, b.ny, b.nz);
+}
+
+template <class T, class Q, class P, int MODE>
 __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
+    constexpr bool STAGED = MODE == EXP_STAGED;
     __shared__ uint64_t s_v[256], s_f[256];
     __shared__ ExpandSmem<T> sm;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
@@ -183,8 +198,9 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t na = STAGED ? (int64_t)min(*p.stage_next, (unsigned long long)p.ent_cap) : min(p.totals[2], p.ent_cap);
     const int64_t nblocks = (na + XW - 1) / XW;
-    const int64_t np = npieces(p);
+    const int64_t np = p.pstride;
     const uint64_t pmask = (1ull << POS_BITS) - 1;
+    const Tabs tb = tabs_of(p);
     __syncthreads();
 
     for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
@@ -202,6 +218,7 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
                 const T *src = (const T *)p.ent_val + 8 * e;
 #pragma unroll
                 for (int k = 0; k < 8; k++) sm.val[k][tid] = src[k];
+                if (MODE == EXP_BATCH) sm.vol[tid] = p.ent_vol[e];
                 if (STAGED) {
                     const uint2 rk = p.ent_rank[e];
                     const int z = (int)(pos >> (2 * POS_BITS));
@@ -265,18 +282,20 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
             const uint64_t pos = sm.pos[j];
             const int ed = (int)((s_v[sm.cs[j]] >> (4 * k)) & 15u);
             const int g = edge_info(ed);
-            vertex_task<T, Q, P>(p, ed, (int)(pos & pmask), (int)((pos >> POS_BITS) & pmask),
+            vertex_task<T, Q, P>(p, MODE == EXP_BATCH ? batch_tabs(p, sm.vol[j]) : tb, ed, (int)(pos & pmask),
+                                 (int)((pos >> POS_BITS) & pmask),
                                  (int)(pos >> (2 * POS_BITS)), sm.val[g & 7][j], sm.val[(g >> 3) & 7][j], sm.vb[j] + k);
         }
         for (int t = tid; t < F; t += XW) {
             const int j = sm.fmap[t];
             const int k = t - sm.fs[j];
             const unsigned s = (unsigned)(s_f[sm.cs[j]] >> (12 * k));
-            const int64_t vb = sm.vb[j];
+            // 1-based within the volume
+            const int64_t vb = sm.vb[j] + 1 - (MODE == EXP_BATCH ? p.vol_off[2 * sm.vol[j]] : 0);
             int64_t *o = p.faces + 3 * (sm.fb[j] + k);
-            o[0] = vb + (s & 15u) + 1;
-            o[1] = vb + ((s >> 4) & 15u) + 1;
-            o[2] = vb + ((s >> 8) & 15u) + 1;
+            o[0] = vb + (s & 15u);
+            o[1] = vb + ((s >> 4) & 15u);
+            o[2] = vb + ((s >> 8) & 15u);
         }
         __syncthreads();
     }

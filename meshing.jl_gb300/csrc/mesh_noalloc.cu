@@ -63,49 +63,6 @@ cudaError_t scratch_address(void **out) {
     return cudaSuccess;
 }
 
-// LinRange node coordinates, spacings and their float forms, computed on the
-// device with the host path's arithmetic: L((1 - t)*a + t*b), t = i/(n-1), every
-// operation rounded separately.
-__global__ void k_tables(double *tabs, int64_t nx, int64_t ny, int64_t nz, double x0, double x1, double y0,
-                         double y1, double z0, double z1, int L32) {
-    const int64_t ntab = nx + ny + nz;
-    double *hp = tabs, *hd = tabs + ntab;
-    float *hpf = (float *)(tabs + 2 * ntab), *hdf = hpf + ntab, *hs = hdf + ntab;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ntab; k += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = k, n = nx;
-        double a = x0, b = x1;
-        if (k >= nx + ny) {
-            i = k - nx - ny; n = nz; a = z0; b = z1;
-        } else if (k >= nx) {
-            i = k - nx; n = ny; a = y0; b = y1;
-        }
-        if (L32) {
-            a = (double)(float)a;
-            b = (double)(float)b;
-        }
-        const double dn = (double)(n > 1 ? n - 1 : 1);
-        auto node = [&](int64_t j) {
-            const double t = __ddiv_rn((double)j, dn);
-            const double v = __dadd_rn(__dmul_rn(__dsub_rn(1.0, t), a), __dmul_rn(t, b));
-            return L32 ? (double)(float)v : v;
-        };
-        const double v = node(i);
-        double d = 0;
-        if (i + 1 < n) {
-            const double v1 = node(i + 1);
-            d = L32 ? (double)__fsub_rn((float)v1, (float)v) : __dsub_rn(v1, v);
-        }
-        hp[k] = v;
-        hd[k] = d;
-        hpf[k] = (float)v;
-        hdf[k] = (float)d;
-        hs[k] = (float)v;
-        hs[ntab + k] = (float)__dsub_rn(v, (double)(float)v);
-        hs[2 * ntab + k] = (float)d;
-        hs[3 * ntab + k] = (float)__dsub_rn(d, (double)(float)d);
-    }
-}
-
 size_t up256(size_t n) { return (n + 255) / 256 * 256; }
 
 }  // namespace
@@ -183,7 +140,7 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     size_t off = 0;
     const size_t o_misc = off;   off += up256((NCNT + 2) * sizeof(int64_t));
     const size_t o_scan = off;   off += up256((size_t)st * NCNT * 8 + 64);
-    const size_t o_tab = off;    off += up256((size_t)ntab * 2 * (8 + 4) + (size_t)ntab * 16);
+    const size_t o_tab = off;    off += up256(table_bytes(ntab));
     const size_t o_cnt = off;    off += up256((size_t)np * NCNT * 4);
     const size_t o_base = off;   off += up256((size_t)np * NCNT * 8);
     const size_t o_flags = off;  off += up256((size_t)P.nchunks * P.tiles_x * P.cy);
@@ -201,13 +158,8 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     P.scan_state = (unsigned long long *)(base + o_scan);
     P.scan_ticket = (unsigned int *)(base + o_scan + (size_t)st * NCNT * 8);
     double *dp = (double *)(base + o_tab);
-    P.xp = dp; P.yp = dp + nx; P.zp = dp + nx + ny;
-    P.dx = dp + ntab; P.dy = P.dx + nx; P.dz = P.dx + nx + ny;
-    float *fp = (float *)(dp + 2 * ntab);
-    P.xpf = fp; P.ypf = fp + nx; P.zpf = fp + nx + ny;
-    P.dxf = fp + ntab; P.dyf = P.dxf + nx; P.dzf = P.dxf + nx + ny;
-    P.split = fp + 2 * ntab;
-    P.ntab = ntab;
+    bind_tables(P, dp, nx, ny, nz);
+    P.pstride = np;
     P.cnt = (uint32_t *)(base + o_cnt);
     P.base = (int64_t *)(base + o_base);
     P.flags = base + o_flags;
@@ -224,9 +176,7 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
 
     // totals, error word and work counter start at zero; the rest is overwritten
     if ((e = cudaMemsetAsync(base + o_misc, 0, (NCNT + 2) * sizeof(int64_t), s)) != cudaSuccess) return MESH_ECUDA;
-    k_tables<<<(int)std::min<int64_t>((ntab + 255) / 256, 1024), 256, 0, s>>>(
-        dp, nx, ny, nz, prm->range[0], prm->range[1], prm->range[2], prm->range[3], prm->range[4], prm->range[5], L32);
-    if ((e = cudaGetLastError()) != cudaSuccess) return MESH_ECUDA;
+    if ((e = launch_tables(dp, nx, ny, nz, prm->range, L32, s)) != cudaSuccess) return MESH_ECUDA;
     if ((e = launch_classify(P, s)) != cudaSuccess) return MESH_ECUDA;
     if ((e = launch_scan(P, s)) != cudaSuccess) return MESH_ECUDA;
     if (P.alg == MESH_ALG_MC) {

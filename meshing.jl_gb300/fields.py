@@ -9,6 +9,7 @@ memory layout of a Julia ``Array{T,3}``, sampled on LinRange nodes.
 * sines            sum_k a_k sin(2pi w_k.p + phi_k) on [0,1]^3, 16 seeded terms
 * ct_like_u16      N(100,20) background + 3 seeded ellipsoidal shells N(1000,50), UInt16
 * primitives_sdf   min-union of 1-8 seeded spheres / boxes on [-1,1]^3
+* batch_volumes    many primitives_sdf volumes of uneven seeded shapes
 """
 import math
 
@@ -121,3 +122,14 @@ def primitives_sdf(shape, prims, dtype=None, device='cuda'):
             d = outside + inside
         f = d if f is None else torch.minimum(f, d)
     return _julia(f.to(dtype).contiguous())
+
+
+def batch_volumes(n=4096, seed=0, lo=16, hi=128, dtype=None, device='cuda'):
+    """`n` volumes, each axis size uniform in lo..hi, each a primitives_sdf of
+    1-8 seeded spheres / boxes on [-1,1]^3 (the batched workload)."""
+    rng = np.random.default_rng(seed)
+    vols = []
+    for _ in range(n):
+        shape = tuple(int(s) for s in rng.integers(lo, hi + 1, 3))
+        vols.append(primitives_sdf(shape, primitives_params(rng), dtype=dtype, device=device))
+    return vols
