@@ -55,7 +55,9 @@ typedef enum {
     MESH_ESTATE = 5,       /* mesh_fill without a preceding successful mesh_count */
     MESH_ECAPACITY = 6,    /* output buffers smaller than the mesh */
     MESH_ETOOLARGE = 7,    /* volume beyond the engine's index limits (more than 2^21 samples on an axis) */
-    MESH_ESCRATCH = 8      /* mesh_extract_noalloc: the call needs more than MESH_NOALLOC_SCRATCH_BYTES */
+    MESH_ESCRATCH = 8,     /* mesh_extract_noalloc: the call needs more than MESH_NOALLOC_SCRATCH_BYTES */
+    MESH_EBUDGET = 9,      /* mesh_server_submit: the request's worst case exceeds the memory budget */
+    MESH_EBUSY = 10        /* mesh_server_submit: the queue is full */
 } mesh_status;
 
 /* Mirrors MarchingCubes{T}(iso) / MarchingTetrahedra{T,E}(iso, eps) plus the
@@ -185,6 +187,45 @@ MESH_API int mesh_batch_knobs(const mesh_batch *b, int *knobs);
 /* Autotuner: times `reps` runs of every candidate of one knob at a time,
  * keeps the fastest, counts again; a text report goes to report[report_len]. */
 MESH_API int mesh_batch_tune(mesh_batch *b, int reps, char *report, int report_len);
+
+/* ---- Serving: continuous batching of extraction requests -------------------
+ * No counterpart in the reference.  Requests name a device-resident volume and
+ * the algorithm parameters (any of the three algorithms, any supported types)
+ * and are answered with exactly the mesh isosurface() gives for them alone.
+ * A loop thread admits queued requests in arrival order into waves whenever a
+ * slot is free and the device pool (budget_bytes, allocated at creation) can
+ * reserve each request's worst-case output: 12 vertices and 5 faces per cell
+ * for Marching Cubes, 7 vertices per node and 12 faces per cell for Marching
+ * Tetrahedra, 1 vertex per cell and 6 faces per node for Naive Surface Nets.
+ * Marching Cubes requests of a wave with the same volume type and iso run as
+ * one batch; waves on different slots overlap on the device.  A request's mesh
+ * stays resident in the pool until mesh_server_release.  Thread-safe. */
+typedef struct mesh_server mesh_server;
+MESH_API int mesh_server_create(int device, int64_t budget_bytes, int slots, int max_wave, int max_queue,
+                                mesh_server **out);
+/* Stops admitting, waits for the waves in flight, frees the pool. */
+MESH_API void mesh_server_destroy(mesh_server *s);
+MESH_API const char *mesh_server_last_error(const mesh_server *s);
+/* Queues a request; *id identifies it.  MESH_EBUDGET: its worst case alone
+ * exceeds the budget; MESH_EBUSY: max_queue requests are waiting. */
+MESH_API int mesh_server_submit(mesh_server *s, const void *vol, int vol_dtype, int64_t nx, int64_t ny, int64_t nz,
+                                const mesh_params *p, int64_t *id);
+/* state: 0 queued, 1 running, 2 done, 3 failed (the return value is then the
+ * failure's status).  When done: counts and device pointers of the vertices
+ * (float(FT) triples) and faces (1-based int64 triples). */
+MESH_API int mesh_server_poll(mesh_server *s, int64_t id, int *state, int64_t *nverts, int64_t *nfaces,
+                              void **verts, int64_t **faces);
+/* As mesh_server_poll after waiting up to timeout_us for the request to end. */
+MESH_API int mesh_server_wait(mesh_server *s, int64_t id, int64_t timeout_us, int *state, int64_t *nverts,
+                              int64_t *nfaces, void **verts, int64_t **faces);
+/* Frees a finished request's output block (its pointers become invalid). */
+MESH_API int mesh_server_release(mesh_server *s, int64_t id);
+/* stats[12]: completed, rejected, failed, p50 / p99 / mean latency in ms
+ * (submission to completion on the device), input samples completed, seconds
+ * from the first submission to the last completion, peak / capacity / current
+ * reserved pool bytes, queued requests. */
+MESH_API int mesh_server_stats(mesh_server *s, double *stats);
+MESH_API int mesh_server_reset_stats(mesh_server *s);
 
 #ifdef __cplusplus
 }

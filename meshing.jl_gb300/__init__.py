@@ -17,7 +17,8 @@ from ._lib import Context, MeshError, MeshParams, load as load_library
 from .api import (MarchingCubes, MarchingTetrahedra, NaiveSurfaceNets, AbstractMeshingAlgorithm, isosurface,
                   isosurface_device, output_float_bits, make_params, default_context)
 from .batch import Batch
+from .serve import Server
 
 __all__ = ['isosurface', 'isosurface_device', 'MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets',
            'AbstractMeshingAlgorithm', 'MeshError', 'Context', 'MeshParams', 'output_float_bits', 'make_params',
-           'default_context', 'load_library', 'Batch']
+           'default_context', 'load_library', 'Batch', 'Server']

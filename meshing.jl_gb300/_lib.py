@@ -12,14 +12,17 @@ LIB_PATH = os.path.join(HERE, '_build', 'libmeshing_gb300.so')
 MESH_DT_U16, MESH_DT_F32, MESH_DT_F64, MESH_DT_I64 = 1, 2, 3, 4
 MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN = 0, 1, 2
 STATUS = {0: 'MESH_OK', 1: 'MESH_EINVAL', 2: 'MESH_ENOMEM', 3: 'MESH_ECUDA', 4: 'MESH_EDEVICE', 5: 'MESH_ESTATE',
-          6: 'MESH_ECAPACITY', 7: 'MESH_ETOOLARGE', 8: 'MESH_ESCRATCH'}
+          6: 'MESH_ECAPACITY', 7: 'MESH_ETOOLARGE', 8: 'MESH_ESCRATCH', 9: 'MESH_EBUDGET', 10: 'MESH_EBUSY'}
 
 # every symbol the header declares
 EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_ctx_set_stream', 'mesh_status_string',
            'mesh_ctx_last_error', 'mesh_output_float_bits', 'mesh_count', 'mesh_fill', 'mesh_extract_device',
            'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times', 'mesh_extract_noalloc',
            'mesh_batch_create', 'mesh_batch_destroy', 'mesh_batch_count', 'mesh_batch_run', 'mesh_batch_sync',
-           'mesh_batch_outputs', 'mesh_batch_set_graph', 'mesh_batch_set_knobs', 'mesh_batch_knobs', 'mesh_batch_tune')
+           'mesh_batch_outputs', 'mesh_batch_set_graph', 'mesh_batch_set_knobs', 'mesh_batch_knobs', 'mesh_batch_tune',
+           'mesh_server_create', 'mesh_server_destroy', 'mesh_server_last_error', 'mesh_server_submit',
+           'mesh_server_poll', 'mesh_server_wait', 'mesh_server_release', 'mesh_server_stats',
+           'mesh_server_reset_stats')
 
 
 class MeshParams(ctypes.Structure):
@@ -72,6 +75,15 @@ def load():
         'mesh_batch_set_knobs': (c_int, [vp, P(c_int)]),
         'mesh_batch_knobs': (c_int, [vp, P(c_int)]),
         'mesh_batch_tune': (c_int, [vp, c_int, ctypes.c_char_p, c_int]),
+        'mesh_server_create': (c_int, [c_int, i64, c_int, c_int, c_int, P(vp)]),
+        'mesh_server_destroy': (None, [vp]),
+        'mesh_server_last_error': (ctypes.c_char_p, [vp]),
+        'mesh_server_submit': (c_int, [vp, vp, c_int, i64, i64, i64, P(MeshParams), P(i64)]),
+        'mesh_server_poll': (c_int, [vp, i64, P(c_int), P(i64), P(i64), P(vp), P(vp)]),
+        'mesh_server_wait': (c_int, [vp, i64, i64, P(c_int), P(i64), P(i64), P(vp), P(vp)]),
+        'mesh_server_release': (c_int, [vp, i64]),
+        'mesh_server_stats': (c_int, [vp, P(ctypes.c_double)]),
+        'mesh_server_reset_stats': (c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

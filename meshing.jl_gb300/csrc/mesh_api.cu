@@ -412,6 +412,8 @@ const char *mesh_status_string(int s) {
     case MESH_ECAPACITY: return "output capacity too small";
     case MESH_ETOOLARGE: return "volume too large";
     case MESH_ESCRATCH: return "needs more scratch than the no-allocation limit";
+    case MESH_EBUDGET: return "worst case exceeds the memory budget";
+    case MESH_EBUSY: return "queue full";
     default: return "unknown status";
     }
 }

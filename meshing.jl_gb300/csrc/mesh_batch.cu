@@ -52,6 +52,57 @@ struct mesh_batch {
     cudaStream_t cap = nullptr;   // capture stream (the legacy default stream cannot be captured)
 };
 
+namespace mesh {
+
+BatchSizes tile_batch(const int64_t *dims, int n, int zs, std::vector<BatchVol> &hv, std::vector<int64_t> &tab_off) {
+    BatchSizes z;
+    hv.assign(n, BatchVol{});
+    tab_off.assign(n, 0);
+    for (int v = 0; v < n; v++) {
+        BatchVol &bv = hv[v];
+        const int64_t nx = dims[3 * v], ny = dims[3 * v + 1], nz = dims[3 * v + 2];
+        bv.nx = nx; bv.ny = ny; bv.nz = nz;
+        bv.item0 = z.items; bv.piece0 = z.pieces; bv.flag0 = z.nflags; bv.stile0 = (int32_t)z.stiles;
+        tab_off[v] = z.tdoubles;
+        if (nx < 2 || ny < 2 || nz < 2) {  // no cells: an empty mesh
+            bv.zs = ZC; bv.chunks_per_seg = 1;
+            continue;
+        }
+        bv.cx = (int32_t)(nx - 1); bv.cy = (int32_t)(ny - 1); bv.cz = (int32_t)(nz - 1);
+        bv.tiles_x = (bv.cx + TILE_X - 1) / TILE_X;
+        bv.tiles_y = (bv.cy + WY - 1) / WY;
+        const int whole = (bv.cz + ZC - 1) / ZC * ZC;
+        bv.zs = zs > 0 ? std::min(whole, (zs + ZC - 1) / ZC * ZC) : whole;
+        bv.nseg = (bv.cz + bv.zs - 1) / bv.zs;
+        bv.chunks_per_seg = bv.zs / ZC;
+        bv.nchunks = bv.nseg * bv.chunks_per_seg;
+        z.items += (int64_t)bv.tiles_x * bv.tiles_y * bv.nseg;
+        z.pieces += (int64_t)bv.nseg * bv.cy * bv.cx;
+        z.nflags += (int64_t)bv.nchunks * bv.tiles_x * bv.cy;
+        z.stiles += (bv.cx + 31) / 32;
+        const int64_t ntab = nx + ny + nz;
+        z.max_ntab = std::max(z.max_ntab, ntab);
+        z.tdoubles += (int64_t)((table_bytes(ntab) + 255) / 256 * 32);  // 256-byte aligned blocks
+    }
+    return z;
+}
+
+void batch_owners(const std::vector<BatchVol> &hv, const BatchSizes &z, std::vector<uint32_t> &ivol,
+                  std::vector<uint32_t> &svol) {
+    ivol.resize((size_t)z.items);
+    svol.resize((size_t)z.stiles);
+    for (size_t v = 0; v < hv.size(); v++) {
+        const BatchVol &bv = hv[v];
+        if (!bv.cx) continue;
+        const int64_t ni = (int64_t)bv.tiles_x * bv.tiles_y * bv.nseg;
+        std::fill(ivol.begin() + bv.item0, ivol.begin() + bv.item0 + ni, (uint32_t)v);
+        const int ns = (bv.cx + 31) / 32;
+        std::fill(svol.begin() + bv.stile0, svol.begin() + bv.stile0 + ns, (uint32_t)v);
+    }
+}
+
+}  // namespace mesh
+
 namespace {
 
 void drop_graph(mesh_batch *b) {
@@ -69,37 +120,11 @@ int build_plan(mesh_batch *b) {
     set_types(P, b->T, &b->prm, &b->Q64, &b->A64, &b->P64);
     const int L32 = b->prm.range_type == MESH_DT_F32;
     const int n = b->n;
-    b->hv.assign(n, BatchVol{});
-    std::vector<int64_t> tab_off(n);
-    int64_t items = 0, pieces = 0, nflags = 0, tdoubles = 0, max_ntab = 1;
-    int64_t stiles = 0;
-    for (int v = 0; v < n; v++) {
-        BatchVol &bv = b->hv[v];
-        const int64_t nx = b->dims[3 * v], ny = b->dims[3 * v + 1], nz = b->dims[3 * v + 2];
-        bv.vol = b->vols[v];
-        bv.nx = nx; bv.ny = ny; bv.nz = nz;
-        bv.item0 = items; bv.piece0 = pieces; bv.flag0 = nflags; bv.stile0 = (int32_t)stiles;
-        tab_off[v] = tdoubles;
-        if (nx < 2 || ny < 2 || nz < 2) {  // no cells: an empty mesh
-            bv.zs = ZC; bv.chunks_per_seg = 1;
-            continue;
-        }
-        bv.cx = (int32_t)(nx - 1); bv.cy = (int32_t)(ny - 1); bv.cz = (int32_t)(nz - 1);
-        bv.tiles_x = (bv.cx + TILE_X - 1) / TILE_X;
-        bv.tiles_y = (bv.cy + WY - 1) / WY;
-        const int whole = (bv.cz + ZC - 1) / ZC * ZC;
-        bv.zs = b->zs > 0 ? std::min(whole, (b->zs + ZC - 1) / ZC * ZC) : whole;
-        bv.nseg = (bv.cz + bv.zs - 1) / bv.zs;
-        bv.chunks_per_seg = bv.zs / ZC;
-        bv.nchunks = bv.nseg * bv.chunks_per_seg;
-        items += (int64_t)bv.tiles_x * bv.tiles_y * bv.nseg;
-        pieces += (int64_t)bv.nseg * bv.cy * bv.cx;
-        nflags += (int64_t)bv.nchunks * bv.tiles_x * bv.cy;
-        stiles += (bv.cx + 31) / 32;
-        const int64_t ntab = nx + ny + nz;
-        max_ntab = std::max(max_ntab, ntab);
-        tdoubles += (int64_t)((table_bytes(ntab) + 255) / 256 * 32);  // 256-byte aligned blocks
-    }
+    std::vector<int64_t> tab_off;
+    const BatchSizes z = tile_batch(b->dims.data(), n, b->zs, b->hv, tab_off);
+    for (int v = 0; v < n; v++) b->hv[v].vol = b->vols[v];
+    const int64_t items = z.items, pieces = z.pieces, nflags = z.nflags, tdoubles = z.tdoubles, stiles = z.stiles;
+    const int64_t max_ntab = z.max_ntab;
     if (items >= ((int64_t)1 << 31) || stiles >= ((int64_t)1 << 31))
         return fail(c, MESH_ETOOLARGE, "batch has too many work items");
 
@@ -119,7 +144,8 @@ int build_plan(mesh_batch *b) {
 
     // per-volume tables, item and scan-tile owners
     std::vector<TabJob> jobs;
-    std::vector<uint32_t> ivol((size_t)items), svol((size_t)stiles);
+    std::vector<uint32_t> ivol, svol;
+    batch_owners(b->hv, z, ivol, svol);
     for (int v = 0; v < n; v++) {
         BatchVol &bv = b->hv[v];
         bv.tabs = (const double *)b->tabs.ptr + tab_off[v];
@@ -129,10 +155,6 @@ int build_plan(mesh_batch *b) {
         j.nx = bv.nx; j.ny = bv.ny; j.nz = bv.nz;
         for (int k = 0; k < 6; k++) j.range[k] = b->ranges[6 * v + k];
         jobs.push_back(j);
-        const int64_t ni = (int64_t)bv.tiles_x * bv.tiles_y * bv.nseg;
-        std::fill(ivol.begin() + bv.item0, ivol.begin() + bv.item0 + ni, (uint32_t)v);
-        const int ns = (bv.cx + 31) / 32;
-        std::fill(svol.begin() + bv.stile0, svol.begin() + bv.stile0 + ns, (uint32_t)v);
     }
     // plan building is off the hot path: plain synchronous uploads
     if ((e = cudaMemcpy(b->dvols.ptr, b->hv.data(), sizeof(BatchVol) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||

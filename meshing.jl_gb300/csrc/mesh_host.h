@@ -87,4 +87,15 @@ int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_
 // Float64, P64: positions in Float64), output eltype and the exact thresholds.
 void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P64);
 
+// Tiling of a batch of volumes of sizes dims[3i..3i+2] with `zs` z cells per
+// work item (0 = whole columns): the descriptors (without device pointers),
+// each volume's table block offset in doubles, and the totals.
+struct BatchSizes {
+    int64_t items = 0, pieces = 0, nflags = 0, tdoubles = 0, stiles = 0, max_ntab = 1;
+};
+BatchSizes tile_batch(const int64_t *dims, int n, int zs, std::vector<BatchVol> &hv, std::vector<int64_t> &tab_off);
+// The volume of every work item and scan tile.
+void batch_owners(const std::vector<BatchVol> &hv, const BatchSizes &z, std::vector<uint32_t> &ivol,
+                  std::vector<uint32_t> &svol);
+
 }  // namespace mesh

@@ -99,17 +99,23 @@ struct Plan {
     int64_t *vol_off;
     int64_t nitems;
     int32_t nvols, nstiles;
+    int32_t vol_outputs;  // 1: every volume writes to its own BatchVol::verts / faces
 };
 
 // One volume of a batch.  Its work items, pieces, activity bytes and scan
 // tiles are ranges of the batch's arrays starting at item0, piece0, flag0 and
 // stile0; its coordinate tables are a block at `tabs` (k_tables.cu layout).
+// With Plan::vol_outputs its mesh goes to its own verts / faces (room for
+// vcap / fcap) instead of the batch's concatenated outputs.
 struct BatchVol {
     const void *vol;
     const double *tabs;
     int64_t nx, ny, nz;
     int32_t cx, cy, cz, tiles_x, tiles_y, nseg, zs, chunks_per_seg, nchunks, stile0;
     int64_t item0, piece0, flag0;
+    void *verts;
+    int64_t *faces;
+    int64_t vcap, fcap;
 };
 
 inline __host__ __device__ int64_t npieces(const Plan &p) { return (int64_t)p.nseg * p.cy * p.cx; }

@@ -65,10 +65,11 @@ template <class P> __device__ __noinline__ F3 still_fp64(const Tabs *tp, int xa,
 }
 
 // The vertex on MC edge e of cell (x, y, z) with corner values va (start) and
-// vbv (end), written to verts[out]; node coordinates from the volume's tables tb.
+// vbv (end), written to vertex `out` of vout; node coordinates from the
+// volume's tables tb.
 template <class T, class Q, class P>
 __device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e, int x, int y, int z, T va, T vbv,
-                                            int64_t out) {
+                                            void *vout, int64_t out) {
     const int g = edge_info(e);
     const int a = g & 7, ax = (g >> 6) & 3, neg = (g >> 8) & 1;
     const int xa = x + cdx(a), ya = y + cdy(a), za = z + cdz(a);
@@ -92,7 +93,7 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e
             o1 = (double)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
             o2 = (double)Ar<P>::add((P)o2, Ar<P>::mul(m, P(0)));
         }
-        double *o = (double *)p.verts + 3 * out;
+        double *o = (double *)vout + 3 * out;
         o[0] = ax == 0 ? (double)rm : o0;
         o[1] = ax == 1 ? (double)rm : o1;
         o[2] = ax == 2 ? (double)rm : o2;
@@ -107,7 +108,7 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e
             o1 = (float)Ar<P>::add((P)o1, Ar<P>::mul(m, P(0)));
             o2 = (float)Ar<P>::add((P)o2, Ar<P>::mul(m, P(0)));
         }
-        float *o = (float *)p.verts + 3 * out;
+        float *o = (float *)vout + 3 * out;
         o[0] = ax == 0 ? fr : o0;
         o[1] = ax == 1 ? fr : o1;
         o[2] = ax == 2 ? fr : o2;
@@ -129,7 +130,7 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e
         }
         F3 ov = {{__ldg(tb.xpf + xa), __ldg(tb.ypf + ya), __ldg(tb.zpf + za)}};
         if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f) ov = still_fp64<P>(&tb, xa, ya, za, (double)mu);
-        float *o = (float *)p.verts + 3 * out;
+        float *o = (float *)vout + 3 * out;
         o[0] = ax == 0 ? fr : ov.v[0];
         o[1] = ax == 1 ? fr : ov.v[1];
         o[2] = ax == 2 ? fr : ov.v[2];
@@ -282,9 +283,20 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
             const uint64_t pos = sm.pos[j];
             const int ed = (int)((s_v[sm.cs[j]] >> (4 * k)) & 15u);
             const int g = edge_info(ed);
+            void *vout = p.verts;
+            int64_t out = sm.vb[j] + k;
+            if (MODE == EXP_BATCH && p.vol_outputs) {  // the volume's own outputs
+                const BatchVol &b = p.bvols[sm.vol[j]];
+                out -= p.vol_off[2 * sm.vol[j]];
+                vout = b.verts;
+                if (out >= b.vcap) {
+                    atomicOr(p.err, ERR_CAPACITY);
+                    continue;
+                }
+            }
             vertex_task<T, Q, P>(p, MODE == EXP_BATCH ? batch_tabs(p, sm.vol[j]) : tb, ed, (int)(pos & pmask),
-                                 (int)((pos >> POS_BITS) & pmask),
-                                 (int)(pos >> (2 * POS_BITS)), sm.val[g & 7][j], sm.val[(g >> 3) & 7][j], sm.vb[j] + k);
+                                 (int)((pos >> POS_BITS) & pmask), (int)(pos >> (2 * POS_BITS)), sm.val[g & 7][j],
+                                 sm.val[(g >> 3) & 7][j], vout, out);
         }
         for (int t = tid; t < F; t += XW) {
             const int j = sm.fmap[t];
@@ -293,6 +305,15 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
             // 1-based within the volume
             const int64_t vb = sm.vb[j] + 1 - (MODE == EXP_BATCH ? p.vol_off[2 * sm.vol[j]] : 0);
             int64_t *o = p.faces + 3 * (sm.fb[j] + k);
+            if (MODE == EXP_BATCH && p.vol_outputs) {
+                const BatchVol &b = p.bvols[sm.vol[j]];
+                const int64_t lf = sm.fb[j] + k - p.vol_off[2 * sm.vol[j] + 1];
+                if (lf >= b.fcap) {
+                    atomicOr(p.err, ERR_CAPACITY);
+                    continue;
+                }
+                o = b.faces + 3 * lf;
+            }
             o[0] = vb + (s & 15u);
             o[1] = vb + ((s >> 4) & 15u);
             o[2] = vb + ((s >> 8) & 15u);

@@ -1,0 +1,104 @@
+"""Serving loop (mesh_server_*): continuous batching of mixed requests.
+
+Every request must give exactly the mesh isosurface() gives for it alone,
+whether it ran alone or in a wave with others (Marching Cubes requests of a
+wave share one batch; waves overlap on the device); admission respects the
+memory budget and the queue limit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALG = ('MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets')
+
+
+def requests(torch, pkg, n, seed, lo=6, hi=90):
+    import meshing_gb300.fields as fields
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        shape = tuple(int(s) for s in rng.integers(lo, hi, 3))
+        dt = torch.float32 if rng.random() < 0.5 else torch.float64
+        if rng.random() < 0.5:
+            A = fields.primitives_sdf(shape, fields.primitives_params(rng), dtype=dt)
+        else:
+            A = (torch.rand(shape, device='cuda', dtype=torch.float64) - 0.5).to(dt)
+        a = rng.choice(3, p=[0.6, 0.3, 0.1])
+        iso = np.float32(0) if dt == torch.float32 and rng.random() < 0.7 else 0.0
+        m = pkg.MarchingTetrahedra(iso=iso) if a == 1 else getattr(pkg, ALG[a])(iso=iso)
+        r = ((-1, 1), (-1, 1), (-1, 1)) if rng.random() < 0.7 else ((0.0, 2.0), (-1.5, 1.0), (0.0, 0.5))
+        out.append((A, m, r))
+    return out
+
+
+def same(torch, got, want):
+    return torch.equal(got[1], want[1]) and torch.equal(got[0], want[0])
+
+
+def test_mix_equals_alone_equals_isosurface(pkg, cuda):
+    torch = cuda
+    reqs = requests(torch, pkg, 48, 1)
+    want = [pkg.isosurface(A, m, *r) for A, m, r in reqs]
+    srv = pkg.Server(budget_bytes=6 << 30, slots=2, max_wave=16)
+    # in the mix: everything queued at once, answered in overlapping waves
+    ids = [srv.submit(A, m, *r) for A, m, r in reqs]
+    for i, rid in enumerate(ids):
+        got = srv.result(rid)
+        assert same(torch, got, want[i]), i
+        srv.release(rid)
+    st = srv.stats()
+    assert st['completed'] == len(reqs) and st['failed'] == 0 and st['rejected'] == 0
+    assert st['peak_reserved_bytes'] <= st['pool_bytes']
+    # alone: one request in flight at a time
+    for i, (A, m, r) in enumerate(reqs[:12]):
+        rid = srv.submit(A, m, *r)
+        assert same(torch, srv.result(rid), want[i]), i
+        srv.release(rid)
+    srv.close()
+
+
+def test_admission_waits_for_memory_and_limits_the_queue(pkg, cuda):
+    torch = cuda
+    import meshing_gb300.fields as fields
+    big = fields.sphere_sdf(100, 0.5, dtype=torch.float32)
+    m = pkg.MarchingCubes(iso=np.float32(0))
+    # a 100^3 Marching Cubes request reserves ~(12*12 + 5*24) B per cell for its
+    # outputs plus its batch scratch: room for one at a time
+    srv = pkg.Server(budget_bytes=420 << 20, slots=2, max_wave=4, max_queue=2)
+    a = srv.submit(big, m)
+    va, fa = srv.result(a)                      # done, output still reserved
+    b = srv.submit(big, m)
+    c = srv.submit(big, m)
+    with pytest.raises(pkg.MeshError) as ei:
+        srv.submit(big, m)                      # two waiting: queue full
+    assert ei.value.status == 10  # MESH_EBUSY
+    assert srv.poll(b) == 'queued'              # no memory until a is released
+    want = pkg.isosurface(big, m)
+    assert same(torch, (va, fa), want)
+    srv.release(a)
+    for rid in (b, c):
+        assert same(torch, srv.result(rid), want)
+        srv.release(rid)
+    # a worst case beyond the whole budget is rejected at once
+    huge = fields.sphere_sdf(160, 0.5, dtype=torch.float32)
+    with pytest.raises(pkg.MeshError) as ei:
+        srv.submit(huge, m)
+    assert ei.value.status == 9  # MESH_EBUDGET
+    st = srv.stats()
+    assert st['rejected'] == 2 and st['completed'] == 3
+    srv.close()
+
+
+def test_empty_and_degenerate_requests(pkg, cuda):
+    torch = cuda
+    srv = pkg.Server(budget_bytes=256 << 20)
+    cases = [torch.ones((5, 6, 7), device='cuda'), torch.zeros((1, 8, 8), device='cuda'),
+             -torch.ones((9, 9, 9), device='cuda', dtype=torch.float64)]
+    for A in cases:
+        for m in (pkg.MarchingCubes(), pkg.MarchingTetrahedra(), pkg.NaiveSurfaceNets()):
+            rid = srv.submit(A, m)
+            v, f = srv.result(rid)
+            assert v.shape[0] == 0 and f.shape[0] == 0
+            srv.release(rid)
+    srv.close()
