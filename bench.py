@@ -399,6 +399,102 @@ def run_batched(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args, rank, world):
+    """The serving workload: Poisson arrivals of requests whose cubic size is
+    log-uniform in 32..512, 50/50 Float32 / Float64, fields of the plain
+    (random sines on [0,1]^3) and batched (primitive SDFs on [-1,1]^3)
+    generators, 60/30/10 MarchingCubes / MarchingTetrahedra / NaiveSurfaceNets,
+    answered by the serving loop under a device-memory budget; then 128^3
+    Marching Cubes requests alone, against a batch of the same volumes."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    import meshing_gb300.fields as fields
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(SEED + rank)
+    pool = []
+    for k in range(args.pool):
+        n = int(round(math.exp(rng.uniform(math.log(32), math.log(512)))))
+        dt = torch.float32 if k % 2 == 0 else torch.float64
+        if rng.random() < 0.5:
+            pool.append((fields.sines(n, seed=k, dtype=dt, device='cuda'), ((0, 1),) * 3))
+        else:
+            pool.append((fields.primitives_sdf((n, n, n), fields.primitives_params(rng), dtype=dt), ((-1, 1),) * 3))
+    torch.cuda.synchronize()
+
+    def method(a, dt):
+        iso = np.float32(0) if dt == torch.float32 else 0.0
+        return [pkg.MarchingCubes, pkg.MarchingTetrahedra, pkg.NaiveSurfaceNets][a](iso=iso)
+
+    srv = pkg.Server(budget_bytes=int(args.budget_gb * 1e9), slots=3, max_wave=256)
+    sweep = []
+    for rate in [float(x) for x in args.rates.split(',')]:
+        nreq = int(min(args.requests, max(50, rate * 3)))
+        reqs = []
+        for _ in range(nreq):
+            A, r = pool[int(rng.integers(len(pool)))]
+            reqs.append((A, method(int(rng.choice(3, p=[0.6, 0.3, 0.1])), A.dtype), r))
+        arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        srv.reset_stats()
+        srv.replay(reqs, arr)
+        st = srv.stats()
+        sweep.append({'offered_per_s': rate, 'requests': nreq, 'completed': int(st['completed']),
+                      'rejected': int(st['rejected']), 'failed': int(st['failed']),
+                      'throughput_per_s': st['completed'] / st['wall_s'] if st['wall_s'] else 0,
+                      'gvox_per_s': st['samples'] / st['wall_s'] / 1e9 if st['wall_s'] else 0,
+                      'p50_ms': st['p50_ms'], 'p99_ms': st['p99_ms'], 'mean_ms': st['mean_ms'],
+                      'peak_reserved_gb': st['peak_reserved_bytes'] / 1e9})
+    del pool
+
+    # 128^3 Marching Cubes requests: the serving loop against one batch of them
+    vols = [fields.primitives_sdf((128, 128, 128), fields.primitives_params(rng), dtype=torch.float32)
+            for _ in range(16)]
+    m = pkg.MarchingCubes(iso=np.float32(0))
+    b = pkg.Batch([vols[i % 16] for i in range(256)], m)
+    b.count()
+    b.set_graph(True)
+    for _ in range(3):
+        b.run()
+    b.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        b.run()
+    e1.record()
+    torch.cuda.synchronize()
+    batched = 256 * 128 ** 3 / (e0.elapsed_time(e1) / 10 * 1e-3) / 1e9
+    b.close()
+    uniform = []
+    for rate in [float(x) for x in args.rates128.split(',')]:
+        nreq = int(min(args.requests128, max(200, rate * 2)))
+        reqs = [(vols[int(rng.integers(16))], m, ((-1, 1),) * 3) for _ in range(nreq)]
+        arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        srv.reset_stats()
+        srv.replay(reqs, arr)
+        st = srv.stats()
+        g = st['samples'] / st['wall_s'] / 1e9 if st['wall_s'] else 0
+        uniform.append({'offered_per_s': rate, 'requests': nreq, 'completed': int(st['completed']),
+                        'throughput_per_s': st['completed'] / st['wall_s'] if st['wall_s'] else 0,
+                        'gvox_per_s': g, 'fraction_of_batched': g / batched, 'p50_ms': st['p50_ms'],
+                        'p99_ms': st['p99_ms']})
+    srv.close()
+    if rank != 0:
+        return
+    best = max(sweep, key=lambda x: x['gvox_per_s'])
+    line = {
+        'metric': 'Gvoxels/s (input samples per second), serving loop', 'workload': 'serving',
+        'value': best['gvox_per_s'], 'unit': 'Gvoxels/s', 'n_gpus': world, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32/f64', 'data': 'synthetic',
+        'config': {'workload': 'Poisson arrivals; cubic sizes log-uniform 32..512; 50/50 Float32 / Float64; random '
+                               'sines on [0,1]^3 or primitive SDFs on [-1,1]^3; 60/30/10 MC / MT / NSN; iso 0',
+                   'budget_gb': args.budget_gb, 'slots': 3, 'max_wave': 256, 'volume_pool': args.pool},
+        'sweep': sweep,
+        'uniform_128_mc': {'batched_gvox_per_s': batched, 'points': uniform},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -409,9 +505,16 @@ def main():
     ap.add_argument('--cpu-planes', type=int, default=None,
                     help='z cell planes of the CPU sample (default 128; 32 for --impl reference)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
-    ap.add_argument('--workload', default='plain', choices=['plain', 'batched'],
-                    help='plain: one 1024^3 volume (the headline); batched: many uneven volumes')
+    ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving'],
+                    help='plain: one 1024^3 volume (the headline); batched: many uneven volumes; serving: the '
+                         'serving loop under Poisson arrivals')
     ap.add_argument('--volumes', type=int, default=4096, help='volumes of the batched workload')
+    ap.add_argument('--pool', type=int, default=40, help='serving: distinct resident request volumes')
+    ap.add_argument('--budget-gb', type=float, default=120.0, help='serving: device memory budget')
+    ap.add_argument('--rates', default='50,200,800', help='serving: offered requests per second')
+    ap.add_argument('--requests', type=int, default=1500, help='serving: requests per rate (at most)')
+    ap.add_argument('--rates128', default='2000,10000,40000', help='serving 128^3: offered requests per second')
+    ap.add_argument('--requests128', type=int, default=20000, help='serving 128^3: requests per rate (at most)')
     args = ap.parse_args()
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
@@ -430,6 +533,8 @@ def main():
     try:
         if args.workload == 'batched':
             run_batched(args, rank, world)
+        elif args.workload == 'serving':
+            run_serving(args, rank, world)
         else:
             run_ours(args, rank, world, dist)
     finally:

@@ -226,6 +226,12 @@ MESH_API int mesh_server_release(mesh_server *s, int64_t id);
  * reserved pool bytes, queued requests. */
 MESH_API int mesh_server_stats(mesh_server *s, double *stats);
 MESH_API int mesh_server_reset_stats(mesh_server *s);
+/* Load generator for measurements: submits request i (vols[i] of dtypes[i],
+ * sizes dims[3i..3i+2], params[i]) arrivals_s[i] seconds after the call
+ * starts, releases each request as soon as it ends, and returns when all have
+ * ended.  Rejected submissions count in the stats. */
+MESH_API int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int *dtypes,
+                                const int64_t *dims, const mesh_params *params, const double *arrivals_s);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_c
            'mesh_batch_outputs', 'mesh_batch_set_graph', 'mesh_batch_set_knobs', 'mesh_batch_knobs', 'mesh_batch_tune',
            'mesh_server_create', 'mesh_server_destroy', 'mesh_server_last_error', 'mesh_server_submit',
            'mesh_server_poll', 'mesh_server_wait', 'mesh_server_release', 'mesh_server_stats',
-           'mesh_server_reset_stats')
+           'mesh_server_reset_stats', 'mesh_server_replay')
 
 
 class MeshParams(ctypes.Structure):
@@ -84,6 +84,7 @@ def load():
         'mesh_server_release': (c_int, [vp, i64]),
         'mesh_server_stats': (c_int, [vp, P(ctypes.c_double)]),
         'mesh_server_reset_stats': (c_int, [vp]),
+        'mesh_server_replay': (c_int, [vp, c_int, P(vp), P(c_int), P(i64), P(MeshParams), P(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

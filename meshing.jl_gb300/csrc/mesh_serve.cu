@@ -748,6 +748,57 @@ int mesh_server_stats(mesh_server *s, double *st) {
     return MESH_OK;
 }
 
+int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int *dtypes, const int64_t *dims,
+                       const mesh_params *params, const double *arrivals_s) {
+    if (!s || n < 0 || (n && (!vols || !dtypes || !dims || !params || !arrivals_s))) return MESH_EINVAL;
+    std::vector<int64_t> ids;
+    std::mutex m;
+    std::condition_variable cv;
+    bool done_submitting = false;
+    // releaser: frees every request as soon as it ends, in submission order
+    std::thread rel([&] {
+        size_t k = 0;
+        for (;;) {
+            int64_t id;
+            {
+                std::unique_lock<std::mutex> lk(m);
+                cv.wait(lk, [&] { return k < ids.size() || done_submitting; });
+                if (k == ids.size()) return;
+                id = ids[k++];
+            }
+            if (id <= 0) continue;
+            int st = 0;
+            while (mesh_server_wait(s, id, 1000000, &st, nullptr, nullptr, nullptr, nullptr) == MESH_OK &&
+                   st != RQ_DONE)
+                ;
+            mesh_server_release(s, id);
+        }
+    });
+    const clk::time_point t0 = clk::now();
+    for (int i = 0; i < n; i++) {
+        const clk::time_point due = t0 + std::chrono::duration_cast<clk::duration>(
+                                              std::chrono::duration<double>(arrivals_s[i]));
+        for (;;) {  // sleep through long gaps, spin through short ones
+            const auto left = due - clk::now();
+            if (left <= clk::duration::zero()) break;
+            if (left > std::chrono::microseconds(300)) std::this_thread::sleep_for(left - std::chrono::microseconds(200));
+        }
+        int64_t id = 0;
+        const int rc = mesh_server_submit(s, vols[i], dtypes[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2],
+                                          &params[i], &id);
+        std::lock_guard<std::mutex> lk(m);
+        ids.push_back(rc == MESH_OK ? id : -1);
+        cv.notify_all();
+    }
+    {
+        std::lock_guard<std::mutex> lk(m);
+        done_submitting = true;
+        cv.notify_all();
+    }
+    rel.join();
+    return MESH_OK;
+}
+
 int mesh_server_reset_stats(mesh_server *s) {
     if (!s) return MESH_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);

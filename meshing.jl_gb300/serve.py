@@ -108,6 +108,28 @@ class Server:
         self._check(self._lib.mesh_server_release(self.handle, rid))
         self._live.pop(rid, None)
 
+    def replay(self, reqs, arrivals):
+        """Native load generator: request i = (A, method, (X, Y, Z)) is submitted
+        arrivals[i] seconds after the start and released as soon as it ends;
+        returns when all have ended (see stats())."""
+        import torch
+        n = len(reqs)
+        vols = (ctypes.c_void_p * n)()
+        dts = (ctypes.c_int * n)()
+        dims = (ctypes.c_int64 * (3 * n))()
+        prms = (_lib.MeshParams * n)()
+        keep = []
+        for i, (A, m, r) in enumerate(reqs):
+            t = _torch_julia_layout(A)
+            keep.append(t)
+            vols[i] = t.data_ptr()
+            dts[i] = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}[t.dtype]
+            dims[3 * i:3 * i + 3] = list(t.shape)
+            prms[i] = make_params(m, *r)
+        torch.cuda.synchronize()
+        arr = (ctypes.c_double * n)(*[float(x) for x in arrivals])
+        self._check(self._lib.mesh_server_replay(self.handle, n, vols, dts, dims, prms, arr))
+
     def stats(self):
         st = (ctypes.c_double * 12)()
         self._check(self._lib.mesh_server_stats(self.handle, st))
