@@ -437,14 +437,18 @@ def run_serving(args, rank, world):
             reqs.append((A, method(int(rng.choice(3, p=[0.6, 0.3, 0.1])), A.dtype), r))
         arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
         srv.reset_stats()
+        t0 = time.time()
         srv.replay(reqs, arr)
         st = srv.stats()
+        print('serving mixed %.0f/s: %d requests in %.1f s, %.1f per wave' % (
+            rate, nreq, time.time() - t0, st['requests_per_wave']), file=sys.stderr, flush=True)
         sweep.append({'offered_per_s': rate, 'requests': nreq, 'completed': int(st['completed']),
                       'rejected': int(st['rejected']), 'failed': int(st['failed']),
                       'throughput_per_s': st['completed'] / st['wall_s'] if st['wall_s'] else 0,
                       'gvox_per_s': st['samples'] / st['wall_s'] / 1e9 if st['wall_s'] else 0,
                       'p50_ms': st['p50_ms'], 'p99_ms': st['p99_ms'], 'mean_ms': st['mean_ms'],
-                      'peak_reserved_gb': st['peak_reserved_bytes'] / 1e9})
+                      'peak_reserved_gb': st['peak_reserved_bytes'] / 1e9,
+                      'requests_per_wave': st['requests_per_wave']})
     del pool
 
     # 128^3 Marching Cubes requests: the serving loop against one batch of them
@@ -471,13 +475,16 @@ def run_serving(args, rank, world):
         reqs = [(vols[int(rng.integers(16))], m, ((-1, 1),) * 3) for _ in range(nreq)]
         arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
         srv.reset_stats()
+        t0 = time.time()
         srv.replay(reqs, arr)
         st = srv.stats()
+        print('serving 128^3 %.0f/s: %d requests in %.1f s, %.1f per wave' % (
+            rate, nreq, time.time() - t0, st['requests_per_wave']), file=sys.stderr, flush=True)
         g = st['samples'] / st['wall_s'] / 1e9 if st['wall_s'] else 0
         uniform.append({'offered_per_s': rate, 'requests': nreq, 'completed': int(st['completed']),
                         'throughput_per_s': st['completed'] / st['wall_s'] if st['wall_s'] else 0,
                         'gvox_per_s': g, 'fraction_of_batched': g / batched, 'p50_ms': st['p50_ms'],
-                        'p99_ms': st['p99_ms']})
+                        'p99_ms': st['p99_ms'], 'requests_per_wave': st['requests_per_wave']})
     srv.close()
     if rank != 0:
         return

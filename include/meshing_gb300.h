@@ -220,10 +220,11 @@ MESH_API int mesh_server_wait(mesh_server *s, int64_t id, int64_t timeout_us, in
                               int64_t *nfaces, void **verts, int64_t **faces);
 /* Frees a finished request's output block (its pointers become invalid). */
 MESH_API int mesh_server_release(mesh_server *s, int64_t id);
-/* stats[12]: completed, rejected, failed, p50 / p99 / mean latency in ms
+/* stats[14]: completed, rejected, failed, p50 / p99 / mean latency in ms
  * (submission to completion on the device), input samples completed, seconds
- * from the first submission to the last completion, peak / capacity / current
- * reserved pool bytes, queued requests. */
+ * from the first submission to the last completion, peak / capacity pool
+ * bytes, queued requests, currently reserved pool bytes, waves launched,
+ * requests per wave.  A finished request keeps only its mesh reserved. */
 MESH_API int mesh_server_stats(mesh_server *s, double *stats);
 MESH_API int mesh_server_reset_stats(mesh_server *s);
 /* Load generator for measurements: submits request i (vols[i] of dtypes[i],

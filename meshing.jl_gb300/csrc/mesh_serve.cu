@@ -80,6 +80,14 @@ struct Pool {
         }
         return false;
     }
+    // Frees [o, o + n) of an allocated block (both multiples of GRAIN).
+    void release_range(size_t o, size_t n) {
+        if (!n) return;
+        Block b;
+        b.off = o;
+        b.size = n;
+        release(&b);
+    }
     size_t largest() const {
         size_t m = 0;
         for (auto &f : free_) m = std::max(m, f.second);
@@ -118,7 +126,8 @@ struct Req {
     int out64 = 0;
     int64_t vcap = 0, fcap = 0;
     size_t vbytes = 0;  // bytes of the vertex part of the output block
-    Block out;
+    Block out;          // worst case while queued / running: vertices at 0, faces at vbytes
+    Block keep_v, keep_f;  // after completion: the parts of `out` that hold the mesh
     int state = RQ_QUEUED;
     int status = MESH_OK;
     int64_t nverts = 0, nfaces = 0;
@@ -233,7 +242,7 @@ struct mesh_server {
     std::string msg;
     // statistics
     std::vector<double> lat_ms;
-    int64_t rejected = 0, failed = 0;
+    int64_t rejected = 0, failed = 0, waves = 0, wave_reqs = 0;
     double samples = 0;
     bool have_t0 = false;
     clk::time_point t0, t_last;
@@ -350,6 +359,13 @@ void CUDART_CB wave_done(void *arg) {
             r.state = RQ_DONE;
             r.nverts = nv;
             r.nfaces = nf;
+            // keep only the mesh: the rest of the worst-case block goes back to the pool
+            const size_t vb = up((size_t)nv * 3 * (r.out64 ? 8 : 4)), fb = up((size_t)nf * 24);
+            r.keep_v = Block{r.out.off, vb};
+            r.keep_f = Block{r.out.off + r.vbytes, fb};
+            s->pool.release_range(r.out.off + vb, r.vbytes - vb);
+            s->pool.release_range(r.out.off + r.vbytes + fb, r.out.size - r.vbytes - fb);
+            r.out.size = 0;
             s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_sub).count());
             s->samples += (double)r.dims[0] * r.dims[1] * r.dims[2];
         }
@@ -548,6 +564,9 @@ void loop(mesh_server *s) {
             continue;
         }
         sl.busy = 1;
+        s->waves++;
+        for (auto &g : sl.groups) s->wave_reqs += (int64_t)g.reqs.size();
+        s->wave_reqs += (int64_t)sl.singles.size();
         lk.unlock();
         const int rc = launch_wave(s, sl);
         lk.lock();
@@ -719,6 +738,8 @@ int mesh_server_release(mesh_server *s, int64_t id) {
     if (it->second.state == RQ_QUEUED || it->second.state == RQ_RUNNING)
         return sfail(s, MESH_ESTATE, "request still in flight");
     s->pool.release(&it->second.out);
+    s->pool.release(&it->second.keep_v);
+    s->pool.release(&it->second.keep_f);
     s->reqs.erase(it);
     s->cv.notify_all();
     return MESH_OK;
@@ -745,6 +766,8 @@ int mesh_server_stats(mesh_server *s, double *st) {
     st[9] = (double)s->pool.cap;
     st[10] = (double)s->queue.size();
     st[11] = (double)s->pool.used;
+    st[12] = (double)s->waves;
+    st[13] = s->waves ? (double)s->wave_reqs / s->waves : 0;
     return MESH_OK;
 }
 
@@ -754,7 +777,7 @@ int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int
     std::vector<int64_t> ids;
     std::mutex m;
     std::condition_variable cv;
-    bool done_submitting = false;
+    bool done_submitting = false, stuck = false;
     // releaser: frees every request as soon as it ends, in submission order
     std::thread rel([&] {
         size_t k = 0;
@@ -767,10 +790,16 @@ int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int
                 id = ids[k++];
             }
             if (id <= 0) continue;
-            int st = 0;
+            int st = 0, tries = 0;
+            // a request that has not ended after 600 s is reported, not waited for
             while (mesh_server_wait(s, id, 1000000, &st, nullptr, nullptr, nullptr, nullptr) == MESH_OK &&
-                   st != RQ_DONE)
+                   st != RQ_DONE && ++tries < 600)
                 ;
+            if (st == RQ_QUEUED || st == RQ_RUNNING) {
+                std::lock_guard<std::mutex> lk(m);
+                stuck = true;
+                continue;
+            }
             mesh_server_release(s, id);
         }
     });
@@ -796,14 +825,14 @@ int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int
         cv.notify_all();
     }
     rel.join();
-    return MESH_OK;
+    return stuck ? sfail(s, MESH_EDEVICE, "a replayed request did not end within 600 s") : MESH_OK;
 }
 
 int mesh_server_reset_stats(mesh_server *s) {
     if (!s) return MESH_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
     s->lat_ms.clear();
-    s->rejected = s->failed = 0;
+    s->rejected = s->failed = s->waves = s->wave_reqs = 0;
     s->samples = 0;
     s->have_t0 = false;
     s->pool.peak = s->pool.used;

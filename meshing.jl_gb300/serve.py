@@ -131,10 +131,10 @@ class Server:
         self._check(self._lib.mesh_server_replay(self.handle, n, vols, dts, dims, prms, arr))
 
     def stats(self):
-        st = (ctypes.c_double * 12)()
+        st = (ctypes.c_double * 14)()
         self._check(self._lib.mesh_server_stats(self.handle, st))
         keys = ('completed', 'rejected', 'failed', 'p50_ms', 'p99_ms', 'mean_ms', 'samples', 'wall_s',
-                'peak_reserved_bytes', 'pool_bytes', 'queued', 'reserved_bytes')
+                'peak_reserved_bytes', 'pool_bytes', 'queued', 'reserved_bytes', 'waves', 'requests_per_wave')
         return dict(zip(keys, list(st)))
 
     def reset_stats(self):

@@ -60,33 +60,39 @@ def test_mix_equals_alone_equals_isosurface(pkg, cuda):
 
 def test_admission_waits_for_memory_and_limits_the_queue(pkg, cuda):
     torch = cuda
-    import meshing_gb300.fields as fields
-    big = fields.sphere_sdf(100, 0.5, dtype=torch.float32)
-    m = pkg.MarchingCubes(iso=np.float32(0))
-    # a 100^3 Marching Cubes request reserves ~(12*12 + 5*24) B per cell for its
-    # outputs plus its batch scratch: room for one at a time
-    srv = pkg.Server(budget_bytes=420 << 20, slots=2, max_wave=4, max_queue=2)
-    a = srv.submit(big, m)
-    va, fa = srv.result(a)                      # done, output still reserved
-    b = srv.submit(big, m)
-    c = srv.submit(big, m)
+    gen = torch.Generator(device='cuda').manual_seed(3)
+    dense = torch.rand((100, 100, 100), device='cuda', generator=gen)  # nearly every cell active
+    m = pkg.MarchingCubes(iso=np.float32(0.5))
+    want = pkg.isosurface(dense, m)
+    # W: what one request reserves in flight (worst case); K: what its finished mesh keeps
+    probe = pkg.Server(budget_bytes=4 << 30)
+    rid = probe.submit(dense, m)
+    probe.wait(rid)
+    st = probe.stats()
+    W, K = int(st['peak_reserved_bytes']), int(st['reserved_bytes'])
+    probe.close()
+    assert 0 < K < W
+    # room for one request in flight, but not beside a finished, unreleased mesh
+    srv = pkg.Server(budget_bytes=W + K // 2, slots=2, max_wave=4, max_queue=2)
+    a = srv.submit(dense, m)
+    assert same(torch, srv.result(a), want)   # done, its mesh still reserved
+    b = srv.submit(dense, m)
+    c = srv.submit(dense, m)
     with pytest.raises(pkg.MeshError) as ei:
-        srv.submit(big, m)                      # two waiting: queue full
+        srv.submit(dense, m)                    # two waiting: queue full
     assert ei.value.status == 10  # MESH_EBUSY
     assert srv.poll(b) == 'queued'              # no memory until a is released
-    want = pkg.isosurface(big, m)
-    assert same(torch, (va, fa), want)
     srv.release(a)
-    for rid in (b, c):
+    for rid in (b, c):                          # one at a time, each after the previous release
         assert same(torch, srv.result(rid), want)
         srv.release(rid)
     # a worst case beyond the whole budget is rejected at once
-    huge = fields.sphere_sdf(160, 0.5, dtype=torch.float32)
+    huge = torch.rand((160, 160, 160), device='cuda', generator=gen)
     with pytest.raises(pkg.MeshError) as ei:
         srv.submit(huge, m)
     assert ei.value.status == 9  # MESH_EBUDGET
     st = srv.stats()
-    assert st['rejected'] == 2 and st['completed'] == 3
+    assert st['rejected'] == 2 and st['completed'] == 3 and st['peak_reserved_bytes'] <= st['pool_bytes']
     srv.close()
 
 
