@@ -255,22 +255,23 @@ def run_ours(args, rank, world, dist):
     in_b = vox * 4
     out_b = nv * 12 + nf * 24
     stage = {k: v[0] / max(v[1], 1) for k, v in st.items()}
-    # algorithmic bytes per launch: classify (k_classify) reads every sample once
-    # (4 B); the emit stage -- compaction of the active cells (k_compact_mc, a
-    # second read of the volume) and their expansion (k_expand_mc) -- writes the
-    # mesh (12 B per vertex, 24 B per face); the scan reads 3 u32 counts and
-    # writes 3 int64 bases per piece.  The active-cell list between compaction and
+    # algorithmic bytes per launch (input 4 B per sample, mesh 12 B per vertex and
+    # 24 B per face): classify (k_classify) and compact (k_compact_mc, the second
+    # pass over the volume that lists the active cells) each read every sample;
+    # expand (k_expand_mc) writes the mesh; the scan reads 3 u32 counts and writes
+    # 3 int64 bases per piece.  The active-cell list between compaction and
     # expansion is not counted.
     kern = {
         'classify': {'ms': stage['classify'], 'bytes': in_b, 'kernel': 'k_classify'},
         'scan': {'ms': stage['scan'], 'bytes': float((n - 1) ** 2 * 3 * (4 + 8)), 'kernel': 'k_scan'},
-        'emit': {'ms': stage['emit'] + stage['expand'], 'bytes': float(out_b), 'kernel': 'k_compact_mc + k_expand_mc',
-                 'compact_ms': stage['emit'], 'expand_ms': stage['expand']},
+        'compact': {'ms': stage['emit'], 'bytes': in_b, 'kernel': 'k_compact_mc'},
+        'expand': {'ms': stage['expand'], 'bytes': float(out_b), 'kernel': 'k_expand_mc'},
     }
     for k in kern.values():
         k['gbs'] = k['bytes'] / (k['ms'] * 1e-3) / 1e9 if k['ms'] else None
         k['frac'] = k['gbs'] / peak if k['gbs'] else None
-    dom = 'classify' if kern['classify']['ms'] >= kern['emit']['ms'] else 'emit'
+    # the dominant kernel: the longest launch of the step
+    dom = max(('classify', 'compact', 'expand'), key=lambda k: kern[k]['ms'])
     achieved = kern[dom]['gbs']
     traffic = None
     tpath = os.path.join(ROOT, 'profiles', 'traffic.json')
@@ -506,6 +507,49 @@ def run_serving(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_gyroid(args, rank, world):
+    """MarchingCubes, MarchingTetrahedra and NaiveSurfaceNets, iso 0, on the
+    Float32 gyroid sin x cos y + sin y cos z + sin z cos x over [-3pi, 3pi]^3
+    (`--n` nodes per axis, 256 by default here): device time per call and per
+    stage through mesh_extract_device."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    import meshing_gb300.fields as fields
+    n = args.n if args.n != N_DEFAULT else 256
+    t = fields.gyroid(n, dtype=torch.float32)
+    torch.cuda.synchronize()
+    r = (-3 * math.pi, 3 * math.pi)
+    out = {}
+    for name, m in (('MarchingCubes', pkg.MarchingCubes(iso=0.0)), ('MarchingTetrahedra', pkg.MarchingTetrahedra(iso=0.0)),
+                    ('NaiveSurfaceNets', pkg.NaiveSurfaceNets(iso=0.0))):
+        ctx = pkg.Context(0)
+        v, f = pkg.isosurface(t, m, r, r, r, ctx=ctx)
+        verts, faces = torch.empty_like(v), torch.empty_like(f)
+        for _ in range(args.warmup):
+            pkg.isosurface_device(t, m, r, r, r, verts=verts, faces=faces, ctx=ctx)
+        ctx.sync()
+        ctx.stage_times()
+        ctx.enable_timing(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            pkg.isosurface_device(t, m, r, r, r, verts=verts, faces=faces, ctx=ctx)
+        e1.record()
+        torch.cuda.synchronize()
+        ctx.sync()
+        ms = e0.elapsed_time(e1) / args.steps
+        st = {k: v[0] / max(v[1], 1) for k, v in ctx.stage_times().items() if v[1]}
+        ok = torch.equal(verts, v) and torch.equal(faces, f)
+        out[name] = {'ms_per_call': ms, 'gvox_per_s': n ** 3 / (ms * 1e-3) / 1e9, 'nverts': v.shape[0],
+                     'nfaces': f.shape[0], 'stage_ms': st, 'repeatable': bool(ok)}
+        ctx.close()
+    if rank == 0:
+        print(json.dumps({'metric': 'Gvoxels/s per algorithm', 'workload': 'gyroid', 'n': n, 'dtype': 'f32',
+                          'config': {'workload': 'Float32 %d^3 gyroid over [-3pi,3pi]^3, iso 0.0 (Float64)' % n},
+                          'algorithms': out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -516,7 +560,7 @@ def main():
     ap.add_argument('--cpu-planes', type=int, default=None,
                     help='z cell planes of the CPU sample (default 128; 32 for --impl reference)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
-    ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving'],
+    ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving', 'gyroid'],
                     help='plain: one 1024^3 volume (the headline); batched: many uneven volumes; serving: the '
                          'serving loop under Poisson arrivals')
     ap.add_argument('--volumes', type=int, default=4096, help='volumes of the batched workload')
@@ -546,6 +590,8 @@ def main():
             run_batched(args, rank, world)
         elif args.workload == 'serving':
             run_serving(args, rank, world)
+        elif args.workload == 'gyroid':
+            run_gyroid(args, rank, world)
         else:
             run_ours(args, rank, world, dist)
     finally:

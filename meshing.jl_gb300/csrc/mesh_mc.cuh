@@ -55,12 +55,14 @@ template <class P> __device__ __noinline__ float moving_fp64(double c1, double d
 struct F3 {
     float v[3];
 };
-template <class P> __device__ __noinline__ F3 still_fp64(const Tabs *tp, int xa, int ya, int za, double m) {
-    const Tabs &t = *tp;
+// (node pointers by value: a pointer to the table view would put it on the stack)
+template <class P>
+__device__ __noinline__ F3 still_fp64(const double *xp, const double *yp, const double *zp, const float *xpf,
+                                      const float *ypf, const float *zpf, int xa, int ya, int za, double m) {
     F3 o;
-    o.v[0] = (float)Ar<P>::add(tab<P>(t.xp, t.xpf, xa), Ar<P>::mul((P)m, P(0)));
-    o.v[1] = (float)Ar<P>::add(tab<P>(t.yp, t.ypf, ya), Ar<P>::mul((P)m, P(0)));
-    o.v[2] = (float)Ar<P>::add(tab<P>(t.zp, t.zpf, za), Ar<P>::mul((P)m, P(0)));
+    o.v[0] = (float)Ar<P>::add(tab<P>(xp, xpf, xa), Ar<P>::mul((P)m, P(0)));
+    o.v[1] = (float)Ar<P>::add(tab<P>(yp, ypf, ya), Ar<P>::mul((P)m, P(0)));
+    o.v[2] = (float)Ar<P>::add(tab<P>(zp, zpf, za), Ar<P>::mul((P)m, P(0)));
     return o;
 }
 
@@ -129,7 +131,8 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e
             fr = moving_fp64<P>(__ldg(tp + ia), neg ? -d : d, (double)mu);
         }
         F3 ov = {{__ldg(tb.xpf + xa), __ldg(tb.ypf + ya), __ldg(tb.zpf + za)}};
-        if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f) ov = still_fp64<P>(&tb, xa, ya, za, (double)mu);
+        if (!fin || ov.v[0] == 0.0f || ov.v[1] == 0.0f || ov.v[2] == 0.0f)
+            ov = still_fp64<P>(tb.xp, tb.yp, tb.zp, tb.xpf, tb.ypf, tb.zpf, xa, ya, za, (double)mu);
         float *o = (float *)vout + 3 * out;
         o[0] = ax == 0 ? fr : ov.v[0];
         o[1] = ax == 1 ? fr : ov.v[1];
