@@ -18,8 +18,14 @@
 //
 // Tiling: 30 x-cells (lanes 1..30) plus the -x neighbour (lane 0) by WY
 // y-cells plus the -y neighbour row, one z segment; lane 31 only supplies
-// samples.  Cases and bases of the current and previous z plane live in
-// per-warp shared memory, so neighbour lookups are plain shared loads.
+// samples.  Per z step the warp classifies its cells lane by lane, then
+// stages the step in its shared memory -- the sample values of both planes,
+// the cases and vertex bases of the current and previous plane, each cell's
+// first face -- with the inclusive prefix of the cells' vertex and face
+// counts.  All 32 lanes then work through the step's vertices and faces as
+// dense task lists (task t -> its cell by binary search over the prefix), so
+// a warp instruction serves up to 32 vertices or faces instead of the few
+// active cells of one row.  Neighbour lookups are plain shared loads.
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
@@ -42,10 +48,25 @@ struct MtTables {
     uint8_t shifted[19][8];  // the same lattice edge seen from the cell shifted by -s
 };
 
-struct WarpState {
-    uint32_t cas[2][R][32];
-    long long base[2][R][32];
+// One warp's state of a z step.
+template <class T> struct HaloWarp {
+    T samp[2][R + 1][32];        // samples of plane z (samp[cur ^ 1]) and z+1 (samp[cur])
+    uint32_t cas[2][R][32];      // cases of the cells of planes z-1 (cur ^ 1) and z (cur)
+    long long base[2][R][32];    // their first vertex
+    long long fbase[R][32];      // first face of the cells of plane z
+    uint16_t pv[R * 32], pf[R * 32];  // inclusive prefix of vertex / face tasks over (row, lane)
 };
+
+// First entry of the inclusive prefix a[0..n) above t (a[n-1] > t).
+__device__ __forceinline__ int task_cell(const uint16_t *a, int n, int t) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)a[mid] > t) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
 
 __device__ __forceinline__ unsigned mc_case(unsigned a, unsigned b, unsigned c, unsigned d) {
     return (a & 1u) | ((a >> 1) << 1) | ((b >> 1) << 2) | ((b & 1u) << 3) | ((c & 1u) << 4) | ((c >> 1) << 5) |
@@ -57,18 +78,12 @@ __device__ __forceinline__ unsigned mt_case(unsigned a, unsigned b, unsigned c, 
 }
 
 
-// vertPos (src/marching_tetrahedra.jl:42-55) for voxel edge e of cell (x,y,z);
-// corner values in MT corner order.
+// vertPos (src/marching_tetrahedra.jl:42-55) for voxel edge e of cell (x,y,z)
+// with the values sv, tv at the edge's corners (MT corner order).
 template <class T, class Q, class A, class P>
-__device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int z, const T (&c)[8], P (&r)[3]) {
+__device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int z, T sv, T tv, P (&r)[3]) {
     const int i1 = MT_EDGE_CORNERS[e][0], i2 = MT_EDGE_CORNERS[e][1];
-    T s = c[0], t = c[0];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        if (k == i1) s = c[k];
-        if (k == i2) t = c[k];
-    }
-    const Q q = quotient<Q>(s, t, p);
+    const Q q = quotient<Q>(sv, tv, p);
     const A eps = sizeof(A) == 4 ? (A)p.eps_f : (A)p.eps_d;
     const A hi = sizeof(A) == 4 ? (A)p.hi_f : (A)p.hi_d;
     const A a = jl_min<A>(jl_max<A>((A)q, eps), hi);
@@ -90,8 +105,8 @@ __device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int
 template <class T, class Q, class A, class P, int ALG>
 __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
     extern __shared__ __align__(16) unsigned char smem[];
-    WarpState *ws_all = reinterpret_cast<WarpState *>(smem);
-    MtTables *tb = reinterpret_cast<MtTables *>(smem + sizeof(WarpState) * WARPS);
+    HaloWarp<T> *ws_all = reinterpret_cast<HaloWarp<T> *>(smem);
+    MtTables *tb = reinterpret_cast<MtTables *>(smem + sizeof(HaloWarp<T>) * WARPS);
     if (ALG == MESH_ALG_MT) {
         for (int i = threadIdx.x; i < 256; i += blockDim.x) {
             for (int k = 0; k < 3 * MT_MAX_FACES; k++) tb->faces[i][k] = MT_CASE_FACES[i][k];
@@ -132,10 +147,11 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
     const int wid = threadIdx.x >> 5;
     const int ty = blockIdx.y * WARPS + wid;
     if (ty >= p.tiles_y) return;
-    WarpState &ws = ws_all[wid];
+    HaloWarp<T> &ws = ws_all[wid];
     const int tx = blockIdx.x;
     const int seg = blockIdx.z;
-    const int xs = tx * TILE_XH - 1 + lane;  // sample / cell x of this lane
+    const int x0 = tx * TILE_XH - 1;         // x of lane 0 (the -x neighbour cell)
+    const int xs = x0 + lane;                // sample / cell x of this lane
     const int y0 = ty * WY;                  // first real cell row; row 0 of the tile is y0-1
     const int zbeg = seg * p.zs;
     const int zend = min(zbeg + p.zs, p.cz);
@@ -180,7 +196,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
         return __any_sync(FULL, f != 0);
     };
 
-    // per-cell case and vertex count for the cell of row r between planes (lo, hi)
+    // per-cell case and vertex / face count for the cell of row r between planes (lo, hi)
     auto classify = [&](const uint32_t (&ml)[R + 1], const uint32_t (&mh)[R + 1], int r, int zc, unsigned &cs,
                         int &nv, int &nf) {
         const unsigned a = (ml[r] >> lane) & 3u, b = (ml[r + 1] >> lane) & 3u;
@@ -205,23 +221,18 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
         }
     };
 
-    T lo[R + 1], lon[R + 1];
     uint32_t mlo[R + 1];
     bool have_lo = false;
-    int cur = 0;  // buffer of the current z plane in ws; cur^1 holds z-1
+    int cur = 0;  // buffer of plane z+1 samples / plane z cells; cur ^ 1 holds plane z / plane z-1
 
-    auto load_plane = [&](int zz, T (&v)[R + 1], T (&vn)[R + 1], uint32_t (&m)[R + 1]) {
+    // samples of plane zz into ws.samp[buf] and their row masks
+    auto load_plane = [&](int zz, int buf, uint32_t (&m)[R + 1]) {
 #pragma unroll
         for (int r = 0; r <= R; r++) {
-            v[r] = rowok[r] ? ldv(rowp[r] + sxy * (int64_t)zz) : T(0);
-            vn[r] = shfl_down1(v[r]);
-            m[r] = __ballot_sync(FULL, rowok[r] && below(v[r], p));
+            const T v = rowok[r] ? ldv(rowp[r] + sxy * (int64_t)zz) : T(0);
+            ws.samp[buf][r][lane] = v;
+            m[r] = __ballot_sync(FULL, rowok[r] && below(v, p));
         }
-    };
-
-    auto clear_prev = [&]() {
-#pragma unroll
-        for (int r = 0; r < R; r++) ws.cas[cur ^ 1][r][lane] = 0;
     };
 
     for (int zc0 = zbeg; zc0 < zend; zc0 += ZC) {
@@ -235,12 +246,11 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
             // the cells of plane zc0-1 are needed as -z neighbours: recompute them
             // when they lie in an active chunk of the previous segment, else they
             // are inactive (their chunk was skipped or does not exist)
-            clear_prev();
+            __syncwarp();
             if (zc0 == zbeg && zc0 > 0 && chunk_active(chunk - 1)) {
-                T pl[R + 1], pln[R + 1];
                 uint32_t pm[R + 1];
-                load_plane(zc0 - 1, pl, pln, pm);
-                load_plane(zc0, lo, lon, mlo);
+                load_plane(zc0 - 1, cur, pm);
+                load_plane(zc0, cur ^ 1, mlo);
 #pragma unroll
                 for (int r = 0; r < R; r++) {
                     unsigned cs;
@@ -250,118 +260,179 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                     ws.base[cur ^ 1][r][lane] = bv[r] - nv;
                 }
             } else {
-                load_plane(zc0, lo, lon, mlo);
+#pragma unroll
+                for (int r = 0; r < R; r++) ws.cas[cur ^ 1][r][lane] = 0;
+                load_plane(zc0, cur ^ 1, mlo);
             }
             have_lo = true;
         }
         for (int zc = zc0; zc < zc1; zc++) {
-            T hi[R + 1], hin[R + 1];
             uint32_t mhi[R + 1];
-            load_plane(zc + 1, hi, hin, mhi);
+            load_plane(zc + 1, cur, mhi);
             unsigned cs[R];
             int nvs[R], nfs[R];
+            bool any = false;
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 classify(mlo, mhi, r, zc, cs[r], nvs[r], nfs[r]);
                 ws.cas[cur][r][lane] = cs[r];
                 ws.base[cur][r][lane] = bv[r];
+                ws.fbase[r][lane] = bf[r];
+                any |= r >= 1 && realx && cs[r] != 0u;
             }
-            __syncwarp();
+            if (__any_sync(FULL, any)) {
+                // tasks of the real cells (rows 1.., lanes 1..30): inclusive prefix over (row, lane)
+                int accv = 0, accf = 0;
 #pragma unroll
-            for (int r = 1; r < R; r++) {
-                if (!realx || !cellok[r] || cs[r] == 0u) continue;
-                const int yc = y0 - 1 + r;
-                const int64_t vb = bv[r], fb = bf[r];
-                if (vb + nvs[r] > p.verts_cap || fb + nfs[r] > p.faces_cap) {
-                    atomicOr(p.err, ERR_CAPACITY);
-                    continue;
-                }
-                if (ALG == MESH_ALG_MT) {
-                    // MT corner order: (x,y,z) (x,y+1,z) (x+1,y+1,z) (x+1,y,z), then z+1
-                    const T cv[8] = {lo[r], lo[r + 1], lon[r + 1], lon[r], hi[r], hi[r + 1], hin[r + 1], hin[r]};
-                    const unsigned c = cs[r];
-                    const int bnd = (xs == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
-                    const uint32_t own = p.own[bnd];
-                    const int nt = __popc(tb->touched[c]);
-                    int rank = 0;
-                    for (int k = 0; k < nt; k++) {
-                        const int e = tb->order[c][k];
-                        if (!((own >> e) & 1u)) continue;
-                        P q[3];
-                        mt_point<T, Q, A, P>(p, e, xs, yc, zc, cv, q);
-                        store_vert(p, vb + rank, q[0], q[1], q[2]);
-                        rank++;
+                for (int r = 0; r < R; r++) {
+                    int tv = 0, tf = 0;
+                    if (r >= 1 && realx && cs[r] != 0u) {
+                        if (bv[r] + nvs[r] > p.verts_cap || bf[r] + nfs[r] > p.faces_cap) {
+                            atomicOr(p.err, ERR_CAPACITY);
+                        } else {
+                            tv = nvs[r];
+                            tf = nfs[r];
+                        }
                     }
-                    const int nf = tb->nfaces[c];
-                    for (int f = 0; f < nf; f++) {
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int a = __shfl_up_sync(FULL, tv, o), b = __shfl_up_sync(FULL, tf, o);
+                        if (lane >= o) {
+                            tv += a;
+                            tf += b;
+                        }
+                    }
+                    ws.pv[r * 32 + lane] = (uint16_t)(accv + tv);
+                    ws.pf[r * 32 + lane] = (uint16_t)(accf + tf);
+                    accv += __shfl_sync(FULL, tv, 31);
+                    accf += __shfl_sync(FULL, tf, 31);
+                }
+                __syncwarp();
+                const int lo_b = cur ^ 1, hi_b = cur;
+                // vertices
+                for (int t = lane; t < accv; t += 32) {
+                    const int sc = task_cell(ws.pv, R * 32, t);
+                    const int r = sc >> 5, l = sc & 31;
+                    const int k = t - (sc ? (int)ws.pv[sc - 1] : 0);
+                    const unsigned c = ws.cas[cur][r][l];
+                    const int xc = x0 + l, yc = y0 - 1 + r;
+                    const int64_t vb = ws.base[cur][r][l];
+                    P q[3];
+                    if (ALG == MESH_ALG_MT) {
+                        const int bnd = (xc == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
+                        const uint32_t own = p.own[bnd];
+                        // the k-th owned edge in the cell's first-use order
+                        const int nt = __popc(tb->touched[c]);
+                        int e = 0, seen = 0;
+                        for (int i = 0; i < nt; i++) {
+                            const int ee = tb->order[c][i];
+                            if (!((own >> ee) & 1u)) continue;
+                            if (seen == k) {
+                                e = ee;
+                                break;
+                            }
+                            seen++;
+                        }
+                        // MT corner order: (x,y,z) (x,y+1,z) (x+1,y+1,z) (x+1,y,z), then z+1
+                        const int i1 = MT_EDGE_CORNERS[e][0], i2 = MT_EDGE_CORNERS[e][1];
+                        auto corner = [&](int kk) -> T {
+                            const int dy = (kk & 3) == 1 || (kk & 3) == 2, dx = (kk & 3) >= 2;
+                            return ws.samp[kk >= 4 ? hi_b : lo_b][r + dy][l + dx];
+                        };
+                        mt_point<T, Q, A, P>(p, e, xc, yc, zc, corner(i1), corner(i2), q);
+                        store_vert(p, vb + k, q[0], q[1], q[2]);
+                    } else {
+                        // NSN: the mean of the crossing points on the crossed MC edges
+                        const T cv[8] = {ws.samp[lo_b][r][l],     ws.samp[lo_b][r][l + 1],
+                                         ws.samp[lo_b][r + 1][l + 1], ws.samp[lo_b][r + 1][l],
+                                         ws.samp[hi_b][r][l],     ws.samp[hi_b][r][l + 1],
+                                         ws.samp[hi_b][r + 1][l + 1], ws.samp[hi_b][r + 1][l]};
+                        // crossed MC edges as a bit mask (edges 0-7 join corners e, e+1 of
+                        // their face ring, 8-11 join e-8 and e-4), summed in edge order
+                        unsigned crossed = 0;
+#pragma unroll
+                        for (int e = 0; e < 12; e++) {
+                            const int ea = e < 8 ? (e & 3) + (e & 4) : e - 8;
+                            const int eb = e < 8 ? ((e + 1) & 3) + (e & 4) : e - 4;
+                            crossed |= (((c >> ea) ^ (c >> eb)) & 1u) << e;
+                        }
+                        P sum[3] = {P(0), P(0), P(0)};
+                        const int n = __popc(crossed);
+                        while (crossed) {
+                            const int e = __ffs(crossed) - 1;
+                            crossed &= crossed - 1;
+                            mc_point<T, Q, P>(p, e, xc, yc, zc, cv, q);
+#pragma unroll
+                            for (int kk = 0; kk < 3; kk++) sum[kk] = Ar<P>::add(sum[kk], q[kk]);
+                        }
+                        store_vert(p, vb, Ar<P>::div(sum[0], (P)n), Ar<P>::div(sum[1], (P)n),
+                                   Ar<P>::div(sum[2], (P)n));
+                    }
+                }
+                // faces
+                for (int t = lane; t < accf; t += 32) {
+                    const int sc = task_cell(ws.pf, R * 32, t);
+                    const int r = sc >> 5, l = sc & 31;
+                    const int f = t - (sc ? (int)ws.pf[sc - 1] : 0);
+                    const unsigned c = ws.cas[cur][r][l];
+                    const int xc = x0 + l, yc = y0 - 1 + r;
+                    const int64_t vb = ws.base[cur][r][l];
+                    int64_t *o = p.faces + 3 * (ws.fbase[r][l] + f);
+                    if (ALG == MESH_ALG_MT) {
+                        const int bnd = (xc == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
+                        const uint32_t own = p.own[bnd];
                         int64_t id[3];
+#pragma unroll
                         for (int j = 0; j < 3; j++) {
                             const int e = tb->faces[c][3 * f + j];
-                            const int s = tb->za[e] & ~bnd;
-                            if (s == 0) {
+                            const int sh = tb->za[e] & ~bnd;
+                            if (sh == 0) {
                                 id[j] = vb + __popc(tb->before[c][e] & own) + 1;
                             } else {
-                                const int e2 = tb->shifted[e][s];
-                                const int l2 = lane - (s & 1), r2 = r - ((s >> 1) & 1);
-                                const int b2 = (s & 4) ? (cur ^ 1) : cur;
+                                // owned by the neighbour one step back along the axes of sh
+                                const int e2 = tb->shifted[e][sh];
+                                const int l2 = l - (sh & 1), r2 = r - ((sh >> 1) & 1);
+                                const int b2 = (sh & 4) ? (cur ^ 1) : cur;
                                 const unsigned c2 = ws.cas[b2][r2][l2];
                                 const int64_t base2 = ws.base[b2][r2][l2];
-                                const int bnd2 = ((xs - (s & 1)) == 0) | (((yc - ((s >> 1) & 1)) == 0) << 1) |
-                                                 (((zc - ((s >> 2) & 1)) == 0) << 2);
+                                const int bnd2 = ((xc - (sh & 1)) == 0) | (((yc - ((sh >> 1) & 1)) == 0) << 1) |
+                                                 (((zc - ((sh >> 2) & 1)) == 0) << 2);
                                 id[j] = base2 + __popc(tb->before[c2][e2] & p.own[bnd2]) + 1;
                             }
                         }
-                        int64_t *o = p.faces + 3 * (fb + f);
                         o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
-                    }
-                } else {
-                    // NSN: vertex = mean of the crossing points on the crossed MC edges
-                    const T cv[8] = {lo[r], lon[r], lon[r + 1], lo[r + 1], hi[r], hin[r], hin[r + 1], hi[r + 1]};
-                    const unsigned c = cs[r];
-                    P sum[3] = {P(0), P(0), P(0)};
-                    int n = 0;
-                    for (int e = 0; e < 12; e++) {
-                        const int ea = e < 8 ? (e & 3) + (e & 4) : e - 8;
-                        const int eb = e < 8 ? ((e + 1) & 3) + (e & 4) : e - 4;
-                        if (((c >> ea) & 1u) == ((c >> eb) & 1u)) continue;
-                        P q[3];
-                        mc_point<T, Q, P>(p, e, xs, yc, zc, cv, q);
-#pragma unroll
-                        for (int k = 0; k < 3; k++) sum[k] = Ar<P>::add(sum[k], q[k]);
-                        n++;
-                    }
-                    store_vert(p, vb, Ar<P>::div(sum[0], (P)n), Ar<P>::div(sum[1], (P)n), Ar<P>::div(sum[2], (P)n));
-                    const int64_t C = vb + 1;
-                    const bool xk = xs > 0, yk = yc > 0, zk = zc > 0;
-                    const unsigned s0 = c & 1u;
-                    const int pv = cur ^ 1;
-                    int f = 0;
-                    // +x edge: u = y, w = z
-                    if (s0 != ((c >> 1) & 1u) && yk && zk) {
-                        const int64_t Aa = ws.base[pv][r - 1][lane] + 1, B = ws.base[pv][r][lane] + 1,
-                                      D = ws.base[cur][r - 1][lane] + 1;
-                        int64_t *o = p.faces + 3 * (fb + f);
-                        if (s0) { o[0] = Aa; o[1] = B; o[2] = C; o[3] = Aa; o[4] = C; o[5] = D; }
-                        else { o[0] = Aa; o[1] = C; o[2] = B; o[3] = Aa; o[4] = D; o[5] = C; }
-                        f += 2;
-                    }
-                    // +y edge: u = z, w = x
-                    if (s0 != ((c >> 3) & 1u) && zk && xk) {
-                        const int64_t Aa = ws.base[pv][r][lane - 1] + 1, B = ws.base[cur][r][lane - 1] + 1,
-                                      D = ws.base[pv][r][lane] + 1;
-                        int64_t *o = p.faces + 3 * (fb + f);
-                        if (s0) { o[0] = Aa; o[1] = B; o[2] = C; o[3] = Aa; o[4] = C; o[5] = D; }
-                        else { o[0] = Aa; o[1] = C; o[2] = B; o[3] = Aa; o[4] = D; o[5] = C; }
-                        f += 2;
-                    }
-                    // +z edge: u = x, w = y
-                    if (s0 != ((c >> 4) & 1u) && xk && yk) {
-                        const int64_t Aa = ws.base[cur][r - 1][lane - 1] + 1, B = ws.base[cur][r - 1][lane] + 1,
-                                      D = ws.base[cur][r][lane - 1] + 1;
-                        int64_t *o = p.faces + 3 * (fb + f);
-                        if (s0) { o[0] = Aa; o[1] = B; o[2] = C; o[3] = Aa; o[4] = C; o[5] = D; }
-                        else { o[0] = Aa; o[1] = C; o[2] = B; o[3] = Aa; o[4] = D; o[5] = C; }
-                        f += 2;
+                    } else {
+                        // NSN: the (f/2)-th crossed base edge of the cell, triangle f%2
+                        const unsigned s0 = c & 1u;
+                        const bool xk = xc > 0, yk = yc > 0, zk = zc > 0;
+                        const bool ex[3] = {s0 != ((c >> 1) & 1u) && yk && zk, s0 != ((c >> 3) & 1u) && zk && xk,
+                                            s0 != ((c >> 4) & 1u) && xk && yk};
+                        int kind = 0;
+                        for (int j = f >> 1, q2 = 0; q2 < 3; q2++) {
+                            if (!ex[q2]) continue;
+                            if (j-- == 0) {
+                                kind = q2;
+                                break;
+                            }
+                        }
+                        const int pv = cur ^ 1;
+                        int64_t Aa, B, D;
+                        if (kind == 0) {  // +x edge: u = y, w = z
+                            Aa = ws.base[pv][r - 1][l]; B = ws.base[pv][r][l]; D = ws.base[cur][r - 1][l];
+                        } else if (kind == 1) {  // +y edge: u = z, w = x
+                            Aa = ws.base[pv][r][l - 1]; B = ws.base[cur][r][l - 1]; D = ws.base[pv][r][l];
+                        } else {  // +z edge: u = x, w = y
+                            Aa = ws.base[cur][r - 1][l - 1]; B = ws.base[cur][r - 1][l]; D = ws.base[cur][r][l - 1];
+                        }
+                        const int64_t C = vb + 1;
+                        Aa += 1; B += 1; D += 1;
+                        if (s0) {
+                            if (f & 1) { o[0] = Aa; o[1] = C; o[2] = D; }
+                            else { o[0] = Aa; o[1] = B; o[2] = C; }
+                        } else {
+                            if (f & 1) { o[0] = Aa; o[1] = D; o[2] = C; }
+                            else { o[0] = Aa; o[1] = C; o[2] = B; }
+                        }
                     }
                 }
             }
@@ -371,12 +442,8 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                 bf[r] += nfs[r];
             }
 #pragma unroll
-            for (int r = 0; r <= R; r++) {
-                lo[r] = hi[r];
-                lon[r] = hin[r];
-                mlo[r] = mhi[r];
-            }
-            __syncwarp();
+            for (int r = 0; r <= R; r++) mlo[r] = mhi[r];
+            __syncwarp();  // every lane is done with this step's shared state
             cur ^= 1;
         }
     }
@@ -385,7 +452,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
 template <class T, class Q, class A, class P, int ALG> cudaError_t go(const Plan &p, cudaStream_t s) {
     const int txh = (p.cx + TILE_XH - 1) / TILE_XH;
     dim3 grid(txh, (p.tiles_y + WARPS - 1) / WARPS, p.nseg);
-    const size_t sm = sizeof(WarpState) * WARPS + (ALG == MESH_ALG_MT ? sizeof(MtTables) : 0);
+    const size_t sm = sizeof(HaloWarp<T>) * WARPS + (ALG == MESH_ALG_MT ? sizeof(MtTables) : 0);
     cudaError_t e = cudaFuncSetAttribute(k_emit_halo<T, Q, A, P, ALG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sm);
     if (e != cudaSuccess) return e;
