@@ -189,9 +189,17 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     cudaError_t e;
     const size_t es = T == MESH_DT_U16 ? 2 : T == MESH_DT_F32 ? 4 : 8;
     const size_t vbytes = (size_t)nx * ny * nz * es;
+    c->host_mapped = 0;
+    cudaPointerAttributes pa;
     if (vol_on_device) {
         P.vol = vol;
+    } else if (p->alg == MESH_ALG_MC && c->zerocopy && cudaPointerGetAttributes(&pa, vol) == cudaSuccess &&
+               pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+        // pinned and mapped: the one walk reads it in place, once
+        P.vol = pa.devicePointer;
+        c->host_mapped = 1;
     } else {
+        cudaGetLastError();
         if ((e = c->vol.ensure(vbytes)) != cudaSuccess) return cuda_fail(c, e, "volume buffer");
         if ((e = cudaMemcpyAsync(c->vol.ptr, vol, vbytes, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
             return cuda_fail(c, e, "volume upload");
@@ -295,8 +303,9 @@ bool make_tensor_map(mesh_ctx *c) {
            CUDA_SUCCESS;
 }
 
-// Marching Cubes walked once, classification staging the active cells (opt-in).
-bool one_walk(const mesh_ctx *c) { return c->plan.alg == MESH_ALG_MC && c->one_walk; }
+// Marching Cubes walked once, classification staging the active cells (opt-in;
+// also the form that reads a mapped host volume in place).
+bool one_walk(const mesh_ctx *c) { return c->plan.alg == MESH_ALG_MC && (c->one_walk || c->host_mapped); }
 
 int run_count(mesh_ctx *c) {
     Plan &P = c->plan;
@@ -448,6 +457,8 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     c->want_tma = wt && wt[0] == '1';
     const char *ow = getenv("MESHING_GB300_ONE_WALK");
     c->one_walk = ow && ow[0] == '1';
+    const char *zc = getenv("MESHING_GB300_ZEROCOPY");
+    c->zerocopy = zc && zc[0] == '1';
     *out = c;
     return MESH_OK;
 }

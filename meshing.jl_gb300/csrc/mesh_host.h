@@ -70,6 +70,13 @@ struct mesh_ctx {
     // expanding the cells in walk order scatters the output writes (1024^3 f32:
     // walk 2.24 + expand 1.41 ms vs classify 1.24 + compact 1.18 + expand 0.75 ms).
     int one_walk = 0;
+    // MESHING_GB300_ZEROCOPY=1: a Marching Cubes host volume in pinned, mapped
+    // memory is read in place over the host link (NVLink-C2C) by the one walk
+    // instead of being copied.  Off by default: on GB300 the in-place walk of a
+    // 4 GiB volume ran at the link's ~140 GB/s, no faster than the copy, and the
+    // one-walk expansion costs more (end to end 42.1 vs 33.6 ms at 1024^3).
+    int zerocopy = 0;
+    int host_mapped = 0; // the current plan reads a mapped host volume
     int use_tma = 0;     // the current plan streams the volume through TMA
     CUtensorMap tmap;
     std::vector<cudaEvent_t> ev_free;

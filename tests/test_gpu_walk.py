@@ -102,3 +102,30 @@ def test_count_without_fill_then_new_count(pkg, oracle, cuda, walk_ctx):
     want = oracle.isosurface(B, 'mc', np.float32(0), 1e-3, ((-1, 1),) * 3)
     got = pkg.isosurface(B, pkg.MarchingCubes(iso=np.float32(0)), ctx=ctx)
     assert_same(got, want)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt'])
+def test_pinned_host_volume_read_in_place(pkg, cuda, alg, monkeypatch):
+    # with MESHING_GB300_ZEROCOPY=1 a pinned (mapped) host volume is read in
+    # place over the host link -- for Marching Cubes by the one walk -- and must
+    # give the device path's mesh; without it, it is copied
+    torch = cuda
+    import meshing_gb300.fields as fields
+    t = fields.gyroid(200, dtype=torch.float32)
+    m = pkg.MarchingCubes(iso=np.float32(0.05)) if alg == 'mc' else pkg.MarchingTetrahedra(iso=np.float32(0.05))
+    v1, f1 = pkg.isosurface(t, m)
+    pinned = torch.empty((200, 200, 200), dtype=torch.float32, pin_memory=True)
+    pinned.copy_(t.permute(2, 1, 0))  # Julia layout: x fastest
+    A = pinned.permute(2, 1, 0)
+    monkeypatch.setenv('MESHING_GB300_ZEROCOPY', '1')
+    for ctx in (pkg.Context(0), pkg.Context(0)):  # fresh and reused context
+        for _ in range(2):
+            v2, f2 = pkg.isosurface(A, m, ctx=ctx)
+            assert np.array_equal(f2, f1.cpu().numpy())
+            assert np.array_equal(v2, v1.cpu().numpy())
+        ctx.close()
+    monkeypatch.delenv('MESHING_GB300_ZEROCOPY')
+    ctx = pkg.Context(0)
+    v3, f3 = pkg.isosurface(A, m, ctx=ctx)
+    ctx.close()
+    assert np.array_equal(f3, f1.cpu().numpy()) and np.array_equal(v3, v1.cpu().numpy())
