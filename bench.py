@@ -283,7 +283,7 @@ def run_ours(args, rank, world, dist):
     pipe_gbs = (in_b + out_b) / (ms * 1e-3) / 1e9
     cpu = None
     if world == 1 and not args.no_cpu:
-        planes = args.cpu_planes or 128
+        planes = args.cpu_planes or 600
         cval, cdt, _, _, cvox = cpu_baseline(n, planes)
         cpu = {'value': cval, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port',
                'sample': 'z slab %dx%dx%d of the same field, CPU restatement of MarchingCubes (oracle/oracle.c, '
@@ -558,7 +558,7 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--n', type=int, default=N_DEFAULT, help='grid size per axis (default 1024)')
     ap.add_argument('--cpu-planes', type=int, default=None,
-                    help='z cell planes of the CPU sample (default 128; 32 for --impl reference)')
+                    help='z cell planes of the CPU sample (default 600, about 12 s on one core; 32 per step for --impl reference)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving', 'gyroid'],
                     help='plain: one 1024^3 volume (the headline); batched: many uneven volumes; serving: the '

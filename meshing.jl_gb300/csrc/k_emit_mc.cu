@@ -27,7 +27,10 @@ namespace mesh {
 
 namespace {
 
-constexpr int U = 2;     // z planes loaded ahead (only active chunks are walked)
+constexpr int U = 4;     // z planes loaded ahead (only active chunks are walked)
+// A chunk's last loaded plane becomes the next chunk's first (lov = v[U-1]), so a
+// group of U planes must never straddle a chunk boundary.
+static_assert(ZC % U == 0, "U must divide the activity chunk");
 
 // ---------------------------------------------------------------- K3a ----
 
@@ -159,7 +162,7 @@ __device__ __forceinline__ void compact_tile(const Plan &p, const uint64_t *s_v,
 }
 
 template <class T>
-__global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems) {
+__global__ void __launch_bounds__(256, 2) k_compact_mc(const Plan p, int nitems) {
     __shared__ uint64_t s_v[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
     __syncthreads();
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(256, 3) k_compact_mc(const Plan p, int nitems)
 
 // Batch: the work items of k_classify_batch, in the same order.
 template <class T>
-__global__ void __launch_bounds__(256, 3) k_compact_batch(const Plan p) {
+__global__ void __launch_bounds__(256, 2) k_compact_batch(const Plan p) {
     __shared__ uint64_t s_v[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
     __syncthreads();

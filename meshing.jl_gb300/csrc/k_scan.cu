@@ -78,16 +78,44 @@ __device__ __forceinline__ void scan_body(const Plan &p, int xt, int gt, int nti
     const int64_t j0 = min(L, (int64_t)w * per), j1 = min(L, j0 + per);
     const int64_t np = p.pstride;
 
+    // piece index of emission step j of column x: (seg, y) advance seg fastest
+    const int64_t dseg = (int64_t)p.cy * p.cx, wrap = (int64_t)p.cx - (int64_t)(p.nseg - 1) * dseg;
+    auto first = [&](int &seg) {
+        seg = (int)(j0 % p.nseg);
+        return piece(p, seg, (int)(j0 / p.nseg), x);
+    };
+    auto next = [&](int64_t &i, int &seg) {
+        if (++seg == p.nseg) {
+            seg = 0;
+            i += wrap;
+        } else {
+            i += dseg;
+        }
+    };
+    constexpr int UN = 4;  // steps whose loads are issued together
+
     int64_t sum[NCNT];
 #pragma unroll
     for (int c = 0; c < NCNT; c++) sum[c] = 0;
     if (xok) {
-        int y = (int)(j0 / p.nseg), seg = (int)(j0 % p.nseg);
-        for (int64_t j = j0; j < j1; j++) {
-            const int64_t i = piece(p, seg, y, x);
+        int seg;
+        int64_t i = first(seg), j = j0;
+        for (; j + UN <= j1; j += UN) {
+            int64_t ii[UN];
+#pragma unroll
+            for (int k = 0; k < UN; k++) {
+                ii[k] = i;
+                next(i, seg);
+            }
+#pragma unroll
+            for (int c = 0; c < NCNT; c++)
+#pragma unroll
+                for (int k = 0; k < UN; k++) sum[c] += p.cnt[c * np + ii[k]];
+        }
+        for (; j < j1; j++) {
 #pragma unroll
             for (int c = 0; c < NCNT; c++) sum[c] += p.cnt[c * np + i];
-            if (++seg == p.nseg) { seg = 0; ++y; }
+            next(i, seg);
         }
     }
 #pragma unroll
@@ -123,15 +151,35 @@ __device__ __forceinline__ void scan_body(const Plan &p, int xt, int gt, int nti
         int64_t b[NCNT];
 #pragma unroll
         for (int c = 0; c < NCNT; c++) b[c] = s_xpre[c][lane] + s_part[c][w][lane];
-        int y = (int)(j0 / p.nseg), seg = (int)(j0 % p.nseg);
-        for (int64_t j = j0; j < j1; j++) {
-            const int64_t i = piece(p, seg, y, x);
+        int seg;
+        int64_t i = first(seg), j = j0;
+        for (; j + UN <= j1; j += UN) {
+            int64_t ii[UN];
+            uint32_t v[NCNT][UN];
+#pragma unroll
+            for (int k = 0; k < UN; k++) {
+                ii[k] = i;
+                next(i, seg);
+            }
+#pragma unroll
+            for (int c = 0; c < NCNT; c++)
+#pragma unroll
+                for (int k = 0; k < UN; k++) v[c][k] = p.cnt[c * np + ii[k]];
+#pragma unroll
+            for (int k = 0; k < UN; k++)
+#pragma unroll
+                for (int c = 0; c < NCNT; c++) {
+                    p.base[c * np + ii[k]] = b[c];
+                    b[c] += v[c][k];
+                }
+        }
+        for (; j < j1; j++) {
 #pragma unroll
             for (int c = 0; c < NCNT; c++) {
                 p.base[c * np + i] = b[c];
                 b[c] += p.cnt[c * np + i];
             }
-            if (++seg == p.nseg) { seg = 0; ++y; }
+            next(i, seg);
         }
     }
 }

@@ -35,17 +35,6 @@ namespace {
 
 constexpr int U = 2;  // z planes loaded ahead
 
-// 8 corner values of an entry, stored contiguously.
-template <class T> __device__ __forceinline__ void put8(T *dst, const T (&v)[8]) {
-#pragma unroll
-    for (int k = 0; k < 8; k++) dst[k] = v[k];
-}
-template <> __device__ __forceinline__ void put8<float>(float *dst, const float (&v)[8]) {
-    float4 *d = reinterpret_cast<float4 *>(dst);
-    d[0] = make_float4(v[0], v[1], v[2], v[3]);
-    d[1] = make_float4(v[4], v[5], v[6], v[7]);
-}
-
 template <class T>
 __global__ void __launch_bounds__(256, 3) k_walk_mc(const Plan p) {
     __shared__ uint32_t s_tab[256];  // vertices | faces << 8 of each case
@@ -154,7 +143,7 @@ __global__ void __launch_bounds__(256, 3) k_walk_mc(const Plan p) {
                                            ((unsigned long long)zc << (2 * POS_BITS));
                             p.ent_cs[e] = (uint8_t)cm;
                             const T vals[8] = {a0, a1, b1, b0, c0, c1, d1, d0};
-                            put8<T>((T *)p.ent_val + 8 * e, vals);
+                            store8<T>((T *)p.ent_val + 8 * e, vals);
                             p.ent_rank[e] = make_uint2(cv[r], cf[r]);
                         } else {
                             over = true;

@@ -140,15 +140,49 @@ __device__ __forceinline__ void vertex_task(const Plan &p, const Tabs &tb, int e
     }
 }
 
-// 8 corner values of an entry, stored contiguously.
-template <class T> __device__ __forceinline__ void store8(T *dst, const T (&v)[8]) {
-#pragma unroll
-    for (int k = 0; k < 8; k++) dst[k] = v[k];
-}
+// 8 corner values of an entry, stored contiguously (16-byte aligned: the list's
+// value array starts on a 256-byte boundary and an entry holds 8 values).
+template <class T> __device__ __forceinline__ void store8(T *dst, const T (&v)[8]);
 template <> __device__ __forceinline__ void store8<float>(float *dst, const float (&v)[8]) {
     float4 *d = reinterpret_cast<float4 *>(dst);
     d[0] = make_float4(v[0], v[1], v[2], v[3]);
     d[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+template <> __device__ __forceinline__ void store8<double>(double *dst, const double (&v)[8]) {
+    double2 *d = reinterpret_cast<double2 *>(dst);
+#pragma unroll
+    for (int k = 0; k < 4; k++) d[k] = make_double2(v[2 * k], v[2 * k + 1]);
+}
+template <> __device__ __forceinline__ void store8<uint16_t>(uint16_t *dst, const uint16_t (&v)[8]) {
+    uint4 q;
+    q.x = v[0] | (uint32_t)v[1] << 16;
+    q.y = v[2] | (uint32_t)v[3] << 16;
+    q.z = v[4] | (uint32_t)v[5] << 16;
+    q.w = v[6] | (uint32_t)v[7] << 16;
+    *reinterpret_cast<uint4 *>(dst) = q;
+}
+template <class T> __device__ __forceinline__ void load8(const T *src, T (&v)[8]);
+template <> __device__ __forceinline__ void load8<float>(const float *src, float (&v)[8]) {
+    const float4 a = reinterpret_cast<const float4 *>(src)[0], b = reinterpret_cast<const float4 *>(src)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+template <> __device__ __forceinline__ void load8<double>(const double *src, double (&v)[8]) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double2 a = reinterpret_cast<const double2 *>(src)[k];
+        v[2 * k] = a.x;
+        v[2 * k + 1] = a.y;
+    }
+}
+template <> __device__ __forceinline__ void load8<uint16_t>(const uint16_t *src, uint16_t (&v)[8]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(src);
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[2 * k] = (uint16_t)(w[k] & 0xffffu);
+        v[2 * k + 1] = (uint16_t)(w[k] >> 16);
+    }
 }
 
 // ------------------------------------------------------------ expansion ----
@@ -219,9 +253,10 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
                 sm.cs[tid] = (uint8_t)cs;
                 const unsigned long long pos = p.ent_pos[e];
                 sm.pos[tid] = pos;
-                const T *src = (const T *)p.ent_val + 8 * e;
+                T cv[8];
+                load8<T>((const T *)p.ent_val + 8 * e, cv);
 #pragma unroll
-                for (int k = 0; k < 8; k++) sm.val[k][tid] = src[k];
+                for (int k = 0; k < 8; k++) sm.val[k][tid] = cv[k];
                 if (MODE == EXP_BATCH) sm.vol[tid] = p.ent_vol[e];
                 if (STAGED) {
                     const uint2 rk = p.ent_rank[e];
