@@ -23,7 +23,8 @@ namespace mesh {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int U = 4;  // z planes loaded ahead
+constexpr int U = 4;     // z planes loaded ahead
+constexpr int CWY = WY;  // cell rows per warp tile of the load walk (the TMA walk keeps WY)
 
 // MC corner order (src/marching_cubes.jl:42-49) from the 2-bit (x, x+1) fields
 // of rows y/y+1 in planes z/z+1.
@@ -48,28 +49,28 @@ template <int ALG> __device__ __forceinline__ void load_tables(uint32_t *s_tab) 
     }
 }
 
-// Per-lane running counts of the WY cells (rows) a lane owns, and per-row
+// Per-lane running counts of the NR cells (rows) a lane owns, and per-row
 // activity of the current z chunk (warp-uniform).
-struct Counts {
-    uint32_t v[WY], f[WY], a[WY], act[WY];
+template <int NR> struct Counts {
+    uint32_t v[NR], f[NR], a[NR], act[NR];
 };
 
 // One z step: the cells between the sample planes whose row masks are mlo
 // (plane z) and mhi (plane z+1).
-template <int ALG>
-__device__ __forceinline__ void step(const Plan &p, const uint32_t *s_tab, const uint32_t (&mlo)[WY + 1],
-                                     const uint32_t (&mhi)[WY + 1], uint32_t xval, uint32_t cellm, int lane, int xs,
-                                     int y0, int zc, Counts &c) {
+template <int ALG, int NR>
+__device__ __forceinline__ void step(const Plan &p, const uint32_t *s_tab, const uint32_t (&mlo)[NR + 1],
+                                     const uint32_t (&mhi)[NR + 1], uint32_t xval, uint32_t cellm, int lane, int xs,
+                                     int y0, int zc, Counts<NR> &c) {
     uint32_t all1 = xval, any1 = 0;
 #pragma unroll
-    for (int r = 0; r <= WY; r++) {
+    for (int r = 0; r <= NR; r++) {
         all1 &= mlo[r] & mhi[r];
         any1 |= mlo[r] | mhi[r];
     }
     // warp-uniform early out: every corner of every cell in this step on one side
     if (all1 == xval || any1 == 0) return;
 #pragma unroll
-    for (int r = 0; r < WY; r++) {
+    for (int r = 0; r < NR; r++) {
         // bit l: cell l has corners on both sides (bits l, l+1 of the four masks)
         const uint32_t and4 = mlo[r] & mlo[r + 1] & mhi[r] & mhi[r + 1];
         const uint32_t or4 = mlo[r] | mlo[r + 1] | mhi[r] | mhi[r + 1];
@@ -104,25 +105,27 @@ __device__ __forceinline__ void step(const Plan &p, const uint32_t *s_tab, const
 }
 
 // At the end of an activity chunk: publish one byte per tile row.
+template <int NR>
 __device__ __forceinline__ void chunk_end(const Plan &p, int lane, int tx, int y0, int seg, int zbeg, int zc,
-                                          int zend, Counts &c) {
+                                          int zend, Counts<NR> &c) {
     if (((zc + 1 - zbeg) % ZC) == 0 || zc + 1 == zend) {
         const int chunk = seg * p.chunks_per_seg + (zc - zbeg) / ZC;
         uint8_t mine = 0;
 #pragma unroll
-        for (int r = 0; r < WY; r++) {
+        for (int r = 0; r < NR; r++) {
             if (lane == r) mine = c.act[r] != 0;  // act[] is warp-uniform
             c.act[r] = 0;
         }
-        if (lane < WY && y0 + lane < p.cy) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+        if (lane < NR && y0 + lane < p.cy) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
     }
 }
 
-__device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, int y0, int seg, const Counts &c) {
+template <int NR>
+__device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, int y0, int seg, const Counts<NR> &c) {
     if (!cellx) return;
     const int64_t np = p.pstride;
 #pragma unroll
-    for (int r = 0; r < WY; r++) {
+    for (int r = 0; r < NR; r++) {
         if (y0 + r < p.cy) {
             const int64_t i = piece(p, seg, y0 + r, xs);
             p.cnt[i] = c.v[r];
@@ -137,58 +140,58 @@ __device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, 
 template <class T, int ALG>
 __device__ __forceinline__ void classify_tile(const Plan &p, const uint32_t *s_tab, int lane, int tx, int ty, int seg) {
     const int xs = tx * TILE_X + lane;
-    const int y0 = ty * WY;
+    const int y0 = ty * CWY;
     const int zbeg = seg * p.zs;
     const int zend = min(zbeg + p.zs, p.cz);
     const bool cellx = lane < TILE_X && xs < p.cx;
     const T *vol = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
 
-    bool rowok[WY + 1];
-    const T *rowp[WY + 1];
+    bool rowok[CWY + 1];
+    const T *rowp[CWY + 1];
 #pragma unroll
-    for (int r = 0; r <= WY; r++) {
+    for (int r = 0; r <= CWY; r++) {
         rowok[r] = xs < p.nx && y0 + r < p.ny;
         rowp[r] = rowok[r] ? vol + xs + p.nx * (int64_t)(y0 + r) : vol;
     }
-    Counts c;
+    Counts<CWY> c;
 #pragma unroll
-    for (int r = 0; r < WY; r++) c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
+    for (int r = 0; r < CWY; r++) c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
     // lanes whose sample exists (x < nx): only their bits take part in the uniform test
     const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
     const uint32_t cellm = __ballot_sync(FULL, cellx);
-    uint32_t mlo[WY + 1];
+    uint32_t mlo[CWY + 1];
 #pragma unroll
-    for (int r = 0; r <= WY; r++) {
+    for (int r = 0; r <= CWY; r++) {
         T v = rowok[r] ? ldv(rowp[r] + sxy * zbeg) : T(0);
         mlo[r] = __ballot_sync(FULL, rowok[r] && below(v, p));
     }
 
     for (int z = zbeg; z < zend; z += U) {
-        T v[U][WY + 1];
+        T v[U][CWY + 1];
         const int64_t off = sxy * (int64_t)(z + 1);
         if (z + U <= zend) {
 #pragma unroll
             for (int u = 0; u < U; u++)
 #pragma unroll
-                for (int r = 0; r <= WY; r++) v[u][r] = rowok[r] ? ldv(rowp[r] + off + sxy * u) : T(0);
+                for (int r = 0; r <= CWY; r++) v[u][r] = rowok[r] ? ldv(rowp[r] + off + sxy * u) : T(0);
         } else {
 #pragma unroll
             for (int u = 0; u < U; u++)
 #pragma unroll
-                for (int r = 0; r <= WY; r++)
+                for (int r = 0; r <= CWY; r++)
                     v[u][r] = (rowok[r] && z + 1 + u <= zend) ? ldv(rowp[r] + off + sxy * u) : T(0);
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const int zc = z + u;
             if (zc >= zend) break;  // warp-uniform
-            uint32_t mhi[WY + 1];
+            uint32_t mhi[CWY + 1];
 #pragma unroll
-            for (int r = 0; r <= WY; r++) mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
-            step<ALG>(p, s_tab, mlo, mhi, xval, cellm, lane, xs, y0, zc, c);
+            for (int r = 0; r <= CWY; r++) mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
+            step<ALG, CWY>(p, s_tab, mlo, mhi, xval, cellm, lane, xs, y0, zc, c);
 #pragma unroll
-            for (int r = 0; r <= WY; r++) mlo[r] = mhi[r];
+            for (int r = 0; r <= CWY; r++) mlo[r] = mhi[r];
             chunk_end(p, lane, tx, y0, seg, zbeg, zc, zend, c);
         }
     }
@@ -201,7 +204,7 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
     load_tables<ALG>(s_tab);
     __syncthreads();
     const int ty = blockIdx.y * WARPS + (threadIdx.x >> 5);
-    if (ty >= p.tiles_y) return;  // warp-uniform
+    if (ty * CWY >= p.cy) return;  // warp-uniform
     classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
 }
 
@@ -299,7 +302,7 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
         bool rowok[WY + 1];
 #pragma unroll
         for (int r = 0; r <= WY; r++) rowok[r] = xs < p.nx && y0 + r < p.ny;
-        Counts c;
+        Counts<WY> c;
 #pragma unroll
         for (int r = 0; r < WY; r++) c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
         const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
                                              rowok[r] && below(st[k * PLANE + (w * WY + r) * BX + xoff + lane], p));
                     if (plane > zbeg) {
                         const int zc = plane - 1;
-                        step<ALG>(p, s_tab, mlo, m, xval, cellm, lane, xs, y0, zc, c);
+                        step<ALG, WY>(p, s_tab, mlo, m, xval, cellm, lane, xs, y0, zc, c);
                         chunk_end(p, lane, tx, y0, seg, zbeg, zc, zend, c);
                     }
 #pragma unroll
@@ -346,7 +349,8 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
 }
 
 template <class T> cudaError_t launch_t(const Plan &p, cudaStream_t s) {
-    dim3 grid(p.tiles_x, (p.tiles_y + WARPS - 1) / WARPS, p.nseg);
+    const int ty = (p.cy + CWY - 1) / CWY;  // warp tiles of the load walk along y
+    dim3 grid(p.tiles_x, (ty + WARPS - 1) / WARPS, p.nseg);
     switch (p.alg) {
     case MESH_ALG_MC: k_classify<T, MESH_ALG_MC><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_ALG_MT: k_classify<T, MESH_ALG_MT><<<grid, 32 * WARPS, 0, s>>>(p); break;
