@@ -37,7 +37,8 @@ typedef enum {
     MESH_DT_U16 = 1, /* UInt16 */
     MESH_DT_F32 = 2, /* Float32 */
     MESH_DT_F64 = 3, /* Float64 */
-    MESH_DT_I64 = 4  /* Int64 (iso and range endpoints only) */
+    MESH_DT_I64 = 4, /* Int64 */
+    MESH_DT_I32 = 5  /* Int32 (volumes only) */
 } mesh_dtype;
 
 typedef enum {

@@ -20,7 +20,7 @@ from typing import Any
 import numpy as np
 
 from . import _lib
-from ._lib import (MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN, MESH_DT_F32, MESH_DT_F64, MESH_DT_I64, MESH_DT_U16,
+from ._lib import (MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN, MESH_DT_F32, MESH_DT_F64, MESH_DT_I32, MESH_DT_I64, MESH_DT_U16,
                    Context, MeshParams, check)
 
 
@@ -55,7 +55,8 @@ class NaiveSurfaceNets(AbstractMeshingAlgorithm):
 
 
 _ALG = {MarchingCubes: MESH_ALG_MC, MarchingTetrahedra: MESH_ALG_MT, NaiveSurfaceNets: MESH_ALG_NSN}
-_VOL_DT = {np.dtype(np.uint16): MESH_DT_U16, np.dtype(np.float32): MESH_DT_F32, np.dtype(np.float64): MESH_DT_F64}
+_VOL_DT = {np.dtype(np.uint16): MESH_DT_U16, np.dtype(np.float32): MESH_DT_F32, np.dtype(np.float64): MESH_DT_F64,
+           np.dtype(np.int32): MESH_DT_I32, np.dtype(np.int64): MESH_DT_I64}
 
 
 def _scalar(v, what):
@@ -162,7 +163,7 @@ def _split_args(args):
 def isosurface(A, *args, ctx=None):
     """isosurface(A[, method][, X, Y, Z]) -> (points, faces).
 
-    ``A``: 3-D numpy array or torch tensor indexed [x, y, z], eltype UInt16,
+    ``A``: 3-D numpy array or torch tensor indexed [x, y, z], eltype UInt16, Int32, Int64,
     Float32 or Float64.  numpy (and CPU torch) inputs return numpy arrays;
     CUDA torch inputs return CUDA torch tensors: points (V, 3) of float(FT)
     and faces (F, 3) int64, 1-based.
@@ -178,7 +179,7 @@ def isosurface(A, *args, ctx=None):
             raise ValueError('volume must be 3-D')
         if not A.is_cuda:
             return isosurface(A.numpy(), method, *rest, ctx=ctx)
-        dt = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}.get(A.dtype)
+        dt = _lib.torch_dtype_code(A.dtype)
         if dt is None:
             raise TypeError('unsupported volume eltype %s' % A.dtype)
         t = _torch_julia_layout(A)
@@ -231,7 +232,9 @@ def isosurface_device(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), verts=Non
     import torch
     method = method or MarchingCubes()
     p = make_params(method, X, Y, Z)
-    dt = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}[A.dtype]
+    dt = _lib.torch_dtype_code(A.dtype)
+    if dt is None:
+        raise TypeError('unsupported volume eltype %s' % A.dtype)
     t = _torch_julia_layout(A)
     c = ctx or default_context(t.device.index or 0)
     c.follow_torch(t.device)

@@ -40,9 +40,9 @@ class Batch:
             raise TypeError('batches run MarchingCubes only')
         if not volumes:
             raise ValueError('empty batch')
-        dt = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}.get(volumes[0].dtype)
+        dt = _lib.torch_dtype_code(volumes[0].dtype)
         if dt is None or any(v.dtype != volumes[0].dtype or v.dim() != 3 or not v.is_cuda for v in volumes):
-            raise TypeError('volumes must be 3-D CUDA tensors of one dtype (UInt16, Float32 or Float64)')
+            raise TypeError('volumes must be 3-D CUDA tensors of one dtype (UInt16, Int32, Int64, Float32 or Float64)')
         self._vols = [_torch_julia_layout(v) for v in volumes]  # keeps the memory alive
         self.device = self._vols[0].device
         self.ctx = ctx or default_context(self.device.index or 0)

@@ -386,7 +386,8 @@ cudaError_t launch_classify_tma(const Plan &p, const CUtensorMap &map, cudaStrea
     switch (p.T) {
     case MESH_DT_U16: return launch_tma_t<uint16_t>(p, map, s);
     case MESH_DT_F32: return launch_tma_t<float>(p, map, s);
-    default: return launch_tma_t<double>(p, map, s);
+    case MESH_DT_F64: return launch_tma_t<double>(p, map, s);
+    default: return cudaErrorInvalidValue;  // integer volumes take the load walk
     }
 }
 
@@ -406,6 +407,8 @@ cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: fn = (const void *)k_classify_batch<uint16_t>; break;
     case MESH_DT_F32: fn = (const void *)k_classify_batch<float>; break;
+    case MESH_DT_I32: fn = (const void *)k_classify_batch<int32_t>; break;
+    case MESH_DT_I64: fn = (const void *)k_classify_batch<int64_t>; break;
     default: fn = (const void *)k_classify_batch<double>; break;
     }
     const int grid = (int)std::min<int64_t>(persistent_grid(fn, 32 * WARPS, ctas), (p.nitems + WARPS - 1) / WARPS);
@@ -413,6 +416,8 @@ cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: k_classify_batch<uint16_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_DT_F32: k_classify_batch<float><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    case MESH_DT_I32: k_classify_batch<int32_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    case MESH_DT_I64: k_classify_batch<int64_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
     default: k_classify_batch<double><<<grid, 32 * WARPS, 0, s>>>(p); break;
     }
     return cudaGetLastError();
@@ -422,6 +427,8 @@ cudaError_t launch_classify(const Plan &p, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: return launch_t<uint16_t>(p, s);
     case MESH_DT_F32: return launch_t<float>(p, s);
+    case MESH_DT_I32: return launch_t<int32_t>(p, s);
+    case MESH_DT_I64: return launch_t<int64_t>(p, s);
     default: return launch_t<double>(p, s);
     }
 }

@@ -478,6 +478,8 @@ cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStrea
     switch (p.T) {
     case MESH_DT_U16: return go_t<uint16_t>(p, Q64, A64, P64, s);
     case MESH_DT_F32: return go_t<float>(p, Q64, A64, P64, s);
+    case MESH_DT_I32: return go_t<int32_t>(p, Q64, A64, P64, s);
+    case MESH_DT_I64: return go_t<int64_t>(p, Q64, A64, P64, s);
     default:
         if (p.alg == MESH_ALG_MT) return go<double, double, double, double, MESH_ALG_MT>(p, s);
         return go<double, double, double, double, MESH_ALG_NSN>(p, s);

@@ -264,6 +264,8 @@ cudaError_t launch_compact_batch(const Plan &p, int ctas, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: return compact_batch_t<uint16_t>(p, ctas, s);
     case MESH_DT_F32: return compact_batch_t<float>(p, ctas, s);
+    case MESH_DT_I32: return compact_batch_t<int32_t>(p, ctas, s);
+    case MESH_DT_I64: return compact_batch_t<int64_t>(p, ctas, s);
     default: return compact_batch_t<double>(p, ctas, s);
     }
 }
@@ -272,6 +274,8 @@ cudaError_t launch_expand_batch(const Plan &p, int Q64, int P64, cudaStream_t s)
     switch (p.T) {
     case MESH_DT_U16: return expand_batch_tt<uint16_t>(p, Q64, P64, s);
     case MESH_DT_F32: return expand_batch_tt<float>(p, Q64, P64, s);
+    case MESH_DT_I32: return expand_batch_tt<int32_t>(p, Q64, P64, s);
+    case MESH_DT_I64: return expand_batch_tt<int64_t>(p, Q64, P64, s);
     default: return expand_batch_t<double, double, double>(p, s);
     }
 }
@@ -281,6 +285,8 @@ cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStrea
     switch (p.T) {
     case MESH_DT_U16: return go_t<uint16_t>(p, Q64, P64, stage, s);
     case MESH_DT_F32: return go_t<float>(p, Q64, P64, stage, s);
+    case MESH_DT_I32: return go_t<int32_t>(p, Q64, P64, stage, s);
+    case MESH_DT_I64: return go_t<int64_t>(p, Q64, P64, stage, s);
     default: return go<double, double, double>(p, stage, s);
     }
 }

@@ -211,6 +211,8 @@ cudaError_t launch_walk_mc(const Plan &p, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: return walk_t<uint16_t>(p, s);
     case MESH_DT_F32: return walk_t<float>(p, s);
+    case MESH_DT_I32: return walk_t<int32_t>(p, s);
+    case MESH_DT_I64: return walk_t<int64_t>(p, s);
     default: return walk_t<double>(p, s);
     }
 }
@@ -219,6 +221,8 @@ cudaError_t launch_expand_staged_mc(const Plan &p, int Q64, int P64, cudaStream_
     switch (p.T) {
     case MESH_DT_U16: return expand_tt<uint16_t>(p, Q64, P64, s);
     case MESH_DT_F32: return expand_tt<float>(p, Q64, P64, s);
+    case MESH_DT_I32: return expand_tt<int32_t>(p, Q64, P64, s);
+    case MESH_DT_I64: return expand_tt<int64_t>(p, Q64, P64, s);
     default: return expand_t<double, double, double>(p, s);
     }
 }

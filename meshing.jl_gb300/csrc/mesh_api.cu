@@ -81,7 +81,7 @@ int out_is_f64(const int *tys, int n) {
 
 int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_params *p) {
     if (!p) return fail(c, MESH_EINVAL, "params is NULL");
-    if (T != MESH_DT_U16 && T != MESH_DT_F32 && T != MESH_DT_F64)
+    if (T != MESH_DT_U16 && T != MESH_DT_F32 && T != MESH_DT_F64 && T != MESH_DT_I32 && T != MESH_DT_I64)
         return fail(c, MESH_EINVAL, "unsupported volume dtype %d", T);
     if (p->alg != MESH_ALG_MC && p->alg != MESH_ALG_MT && p->alg != MESH_ALG_NSN)
         return fail(c, MESH_EINVAL, "unknown algorithm %d", p->alg);
@@ -124,7 +124,8 @@ void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P6
     P.alg = p->alg;
     const int I = p->iso_type, E = p->eps_type, Rt = p->range_type;
     const int mt = p->alg == MESH_ALG_MT;
-    *Q64 = T == MESH_DT_F64 || I == MESH_DT_F64 || (T == MESH_DT_U16 && I == MESH_DT_I64);
+    // promote(typeof(iso), T); Int / Int divides in Float64
+    *Q64 = T == MESH_DT_F64 || I == MESH_DT_F64 || (T != MESH_DT_F32 && I == MESH_DT_I64);
     const int L32 = Rt == MESH_DT_F32;
     *A64 = mt ? (*Q64 || E == MESH_DT_F64) : *Q64;
     *P64 = *A64 || !L32;
@@ -142,6 +143,20 @@ void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P6
         double ce = std::ceil(iso);
         if (std::isnan(iso)) ce = 0;
         P.thr_i = (int32_t)std::min(65536.0, std::max(0.0, ce));
+        // Int32 / Int64 data: x < iso  <=>  x < ceil(iso), exact for every Int64 x
+        P.thr_all = 0;
+        if (std::isnan(iso)) {
+            P.thr_l = INT64_MIN;                      // nothing is below NaN
+        } else if (ce >= 9223372036854775808.0) {
+            P.thr_l = INT64_MAX;
+            P.thr_all = 1;                            // beyond every Int64
+        } else if (ce < -9223372036854775808.0) {
+            P.thr_l = INT64_MIN;
+        } else {
+            P.thr_l = (int64_t)ce;
+        }
+        P.iso_int = T == MESH_DT_I64 && I == MESH_DT_I64;
+        P.iso_l = I == MESH_DT_I64 ? (int64_t)iso : 0;
     }
     P.isoq_d = iso;
     P.isoq_f = (float)iso;
@@ -187,7 +202,7 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
         return fail(c, MESH_ETOOLARGE, "grid too large for this volume shape");
 
     cudaError_t e;
-    const size_t es = T == MESH_DT_U16 ? 2 : T == MESH_DT_F32 ? 4 : 8;
+    const size_t es = dtype_size(T);
     const size_t vbytes = (size_t)nx * ny * nz * es;
     c->host_mapped = 0;
     cudaPointerAttributes pa;
@@ -289,7 +304,8 @@ bool make_tensor_map(mesh_ctx *c) {
     switch (P.T) {
     case MESH_DT_U16: bx = TmaBox<uint16_t>::BX; es = 2; dt = CU_TENSOR_MAP_DATA_TYPE_UINT16; break;
     case MESH_DT_F32: bx = TmaBox<float>::BX; es = 4; dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; break;
-    default: bx = TmaBox<double>::BX; es = 8; dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; break;
+    case MESH_DT_F64: bx = TmaBox<double>::BX; es = 8; dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; break;
+    default: return false;  // integer volumes take the load walk
     }
     if (((uintptr_t)P.vol & 15) || ((size_t)P.nx * es) % 16 || P.nx < bx || P.ny < TMA_BY || P.nz < TMA_BZ) return false;
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
@@ -345,7 +361,7 @@ int fetch_misc(mesh_ctx *c) {
 // List of active cells (Marching Cubes), room for `cap` entries.
 int ensure_entries(mesh_ctx *c, int64_t cap) {
     Plan &P = c->plan;
-    const size_t es = P.T == MESH_DT_U16 ? 2 : P.T == MESH_DT_F32 ? 4 : 8;
+    const size_t es = dtype_size(P.T);
     const int64_t nside = cap / ENT_BLOCK + 1;
     auto up = [](size_t n) { return (n + 255) / 256 * 256; };  // every array 256-byte aligned
     const size_t o_val = up((size_t)cap * 8);

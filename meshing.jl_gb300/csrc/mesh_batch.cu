@@ -232,7 +232,7 @@ int count(mesh_batch *b) {
     b->nactive = b->h_misc[2];
     Plan &P = b->P;
     // active-cell list (emission order over the batch) and the outputs, sized exactly
-    const size_t es = b->T == MESH_DT_U16 ? 2 : b->T == MESH_DT_F32 ? 4 : 8;
+    const size_t es = dtype_size(b->T);
     const int64_t cap = b->nactive;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     const size_t o_val = up((size_t)cap * 8);

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "meshing_gb300.h"  // include/ (on the include path)
 
 namespace mesh {
@@ -39,7 +41,12 @@ struct Plan {
     // classification thresholds: v < iso  <=>  v < thr (exact, in the data type)
     float thr_f;
     double thr_d;
-    int32_t thr_i;
+    int32_t thr_i;       // UInt16 data
+    int64_t thr_l;       // Int32 / Int64 data: v < iso  <=>  v < thr_l, or every v (thr_all)
+    int32_t thr_all;
+    // Int64 iso on Int64 data: (iso - v1) is an Int64 difference (wrapping)
+    int64_t iso_l;
+    int32_t iso_int;
     // iso as it enters (iso - v1)/(v2 - v1)
     float isoq_f;
     double isoq_d;
@@ -117,6 +124,11 @@ struct BatchVol {
     int64_t *faces;
     int64_t vcap, fcap;
 };
+
+// Bytes per sample of a volume dtype.
+inline __host__ __device__ size_t dtype_size(int T) {
+    return T == MESH_DT_U16 ? 2 : (T == MESH_DT_F32 || T == MESH_DT_I32) ? 4 : 8;
+}
 
 inline __host__ __device__ int64_t npieces(const Plan &p) { return (int64_t)p.nseg * p.cy * p.cx; }
 
@@ -221,11 +233,20 @@ template <> struct Ar<double> {
 __device__ __forceinline__ bool below(float v, const Plan &p) { return v < p.thr_f; }
 __device__ __forceinline__ bool below(double v, const Plan &p) { return v < p.thr_d; }
 __device__ __forceinline__ bool below(uint16_t v, const Plan &p) { return (int32_t)v < p.thr_i; }
+__device__ __forceinline__ bool below(int32_t v, const Plan &p) { return (int64_t)v < p.thr_l || p.thr_all; }
+__device__ __forceinline__ bool below(int64_t v, const Plan &p) { return v < p.thr_l || p.thr_all; }
 
 // v2 - v1 in the data type (UInt16 wraps), then converted to Q.
 template <class Q> __device__ __forceinline__ Q tdiff(float v2, float v1) { return (Q)__fsub_rn(v2, v1); }
 template <class Q> __device__ __forceinline__ Q tdiff(double v2, double v1) { return (Q)__dsub_rn(v2, v1); }
 template <class Q> __device__ __forceinline__ Q tdiff(uint16_t v2, uint16_t v1) { return (Q)(uint16_t)(v2 - v1); }
+// machine-integer differences wrap; the conversion to Q rounds to nearest
+template <class Q> __device__ __forceinline__ Q tdiff(int32_t v2, int32_t v1) {
+    return (Q)(int32_t)((uint32_t)v2 - (uint32_t)v1);
+}
+template <class Q> __device__ __forceinline__ Q tdiff(int64_t v2, int64_t v1) {
+    return (Q)(int64_t)((unsigned long long)v2 - (unsigned long long)v1);
+}
 
 template <class Q> __device__ __forceinline__ Q isoq(const Plan &p);
 template <> __device__ __forceinline__ float isoq<float>(const Plan &p) { return p.isoq_f; }
@@ -234,7 +255,11 @@ template <> __device__ __forceinline__ double isoq<double>(const Plan &p) { retu
 // (iso - v1) / (v2 - v1) in Julia's promoted types.
 template <class Q, class T> __device__ __forceinline__ Q quotient(T v1, T v2, const Plan &p) {
     Q den = tdiff<Q>(v2, v1);
-    Q num = Ar<Q>::sub(isoq<Q>(p), (Q)v1);
+    Q num;
+    if (std::is_integral<T>::value && sizeof(T) == 8 && p.iso_int)  // Int64 data, Int64 iso: Int64 (iso - v1)
+        num = (Q)(int64_t)((unsigned long long)p.iso_l - (unsigned long long)(int64_t)v1);
+    else
+        num = Ar<Q>::sub(isoq<Q>(p), (Q)v1);
     return Ar<Q>::div(num, den);
 }
 

@@ -161,7 +161,30 @@ template <> __device__ __forceinline__ void store8<uint16_t>(uint16_t *dst, cons
     q.w = v[6] | (uint32_t)v[7] << 16;
     *reinterpret_cast<uint4 *>(dst) = q;
 }
+template <> __device__ __forceinline__ void store8<int32_t>(int32_t *dst, const int32_t (&v)[8]) {
+    int4 *d = reinterpret_cast<int4 *>(dst);
+    d[0] = make_int4(v[0], v[1], v[2], v[3]);
+    d[1] = make_int4(v[4], v[5], v[6], v[7]);
+}
+template <> __device__ __forceinline__ void store8<int64_t>(int64_t *dst, const int64_t (&v)[8]) {
+    longlong2 *d = reinterpret_cast<longlong2 *>(dst);
+#pragma unroll
+    for (int k = 0; k < 4; k++) d[k] = make_longlong2(v[2 * k], v[2 * k + 1]);
+}
 template <class T> __device__ __forceinline__ void load8(const T *src, T (&v)[8]);
+template <> __device__ __forceinline__ void load8<int32_t>(const int32_t *src, int32_t (&v)[8]) {
+    const int4 a = reinterpret_cast<const int4 *>(src)[0], b = reinterpret_cast<const int4 *>(src)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+template <> __device__ __forceinline__ void load8<int64_t>(const int64_t *src, int64_t (&v)[8]) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const longlong2 a = reinterpret_cast<const longlong2 *>(src)[k];
+        v[2 * k] = a.x;
+        v[2 * k + 1] = a.y;
+    }
+}
 template <> __device__ __forceinline__ void load8<float>(const float *src, float (&v)[8]) {
     const float4 a = reinterpret_cast<const float4 *>(src)[0], b = reinterpret_cast<const float4 *>(src)[1];
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;

@@ -134,7 +134,7 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     const int64_t ntab = nx + ny + nz;
     const int64_t np = npieces(P);
     const int st = scan_tiles(P);
-    const size_t es = T == MESH_DT_U16 ? 2 : T == MESH_DT_F32 ? 4 : 8;
+    const size_t es = dtype_size(T);
     const int64_t cap = prm->alg == MESH_ALG_MC ? verts_cap / 3 : 0;  // active MC cells emit >= 3 vertices
     const int64_t nside = cap / ENT_BLOCK + 1;
     size_t off = 0;

@@ -172,7 +172,6 @@ struct GroupLayout {
     int64_t cells = 0;
 };
 
-size_t dtype_bytes(int T) { return T == MESH_DT_U16 ? 2 : T == MESH_DT_F32 ? 4 : 8; }
 
 void layout_group(const std::vector<const Req *> &rs, GroupLayout *L) {
     const int n = (int)rs.size();
@@ -185,7 +184,7 @@ void layout_group(const std::vector<const Req *> &rs, GroupLayout *L) {
     }
     L->z = tile_batch(dims.data(), n, 0, L->hv, L->tab_off);
     const BatchSizes &z = L->z;
-    const size_t es = n ? dtype_bytes(rs[0]->T) : 4;
+    const size_t es = n ? dtype_size(rs[0]->T) : 4;
     size_t o = up(sizeof(BatchVol) * (size_t)std::max(n, 1));
     L->o_ivol = o; o += up(4 * (size_t)z.items + 4);
     L->o_svol = o; o += up(4 * (size_t)z.stiles + 4);
@@ -218,7 +217,7 @@ size_t vol_scratch_bytes(const Req &r) {
         const int64_t tx = (cx + TILE_X - 1) / TILE_X, ty = (cy + WY - 1) / WY, st = (cx + 31) / 32;
         b += 4 * (size_t)(tx * ty) + 4 * (size_t)st + table_bytes(nx + ny + nz) + 256;
         b += (size_t)cy * cx * NCNT * (4 + 8) + (size_t)(zs / ZC) * tx * cy + (size_t)st * NCNT * 8;
-        b += (size_t)cells * (8 + 8 * dtype_bytes(r.T) + 4 + 1) + (size_t)(cells / ENT_BLOCK + 1) * 16;
+        b += (size_t)cells * (8 + 8 * dtype_size(r.T) + 4 + 1) + (size_t)(cells / ENT_BLOCK + 1) * 16;
     }
     return b;
 }

@@ -4,7 +4,7 @@
 Drop-in GPU back end for Meshing.jl.  Loading this module adds methods of
 `Meshing.isosurface` that are more specific than the reference's
 (src/marching_cubes.jl:27, src/marching_tetrahedra.jl:129): dense
-`Array{T,3}` volumes with `T ∈ {UInt16, Float32, Float64}` and iso / eps /
+`Array{T,3}` volumes with `T ∈ {UInt16, Int32, Int64, Float32, Float64}` and iso / eps /
 range endpoints of type Float32, Float64 or Int64 run on the GPU through
 `libmeshing_gb300.so`.  Every other combination (Float16, Int data,
 ForwardDiff.Dual, mixed endpoint types) reaches the reference method through
@@ -44,13 +44,14 @@ struct MeshParams
     range::NTuple{6,Float64}
 end
 
-const DevEl = Union{UInt16,Float32,Float64}
+const DevEl = Union{UInt16,Int32,Int64,Float32,Float64}
 const DevScalar = Union{Float32,Float64,Int64}
 
 dtcode(::Type{UInt16}) = Int32(1)
 dtcode(::Type{Float32}) = Int32(2)
 dtcode(::Type{Float64}) = Int32(3)
 dtcode(::Type{Int64}) = Int32(4)
+dtcode(::Type{Int32}) = Int32(5)
 dtcode(::Type) = Int32(0)
 
 # one context per thread: a context is not thread-safe

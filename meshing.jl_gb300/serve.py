@@ -57,9 +57,9 @@ class Server:
         """Queue isosurface(A, method, X, Y, Z) for CUDA volume A; returns the request id."""
         import torch
         method = method or MarchingCubes()
-        dt = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}.get(A.dtype)
+        dt = _lib.torch_dtype_code(A.dtype)
         if dt is None or A.dim() != 3 or not A.is_cuda:
-            raise TypeError('volume must be a 3-D CUDA tensor of UInt16, Float32 or Float64')
+            raise TypeError('volume must be a 3-D CUDA tensor of UInt16, Int32, Int64, Float32 or Float64')
         t = _torch_julia_layout(A)
         p = make_params(method, X, Y, Z)
         bits = ctypes.c_int()
@@ -123,7 +123,7 @@ class Server:
             t = _torch_julia_layout(A)
             keep.append(t)
             vols[i] = t.data_ptr()
-            dts[i] = {torch.uint16: MESH_DT_U16, torch.float32: MESH_DT_F32, torch.float64: MESH_DT_F64}[t.dtype]
+            dts[i] = _lib.torch_dtype_code(t.dtype)
             dims[3 * i:3 * i + 3] = list(t.shape)
             prms[i] = make_params(m, *r)
         torch.cuda.synchronize()

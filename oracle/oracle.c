@@ -26,6 +26,9 @@
  *   - no fused multiply-add (build with -ffp-contract=off).
  * Float32 operations are done as double operations rounded to float, which is
  * exact for + - * / (double has more than 2*24+2 significand bits).
+ * Int32 / Int64 samples travel as their exact int64 bit pattern inside the
+ * sample slots (only `below` and `quotient` read sample values); their
+ * differences wrap like Julia's machine integers.
  */
 #include <math.h>
 #include <stdint.h>
@@ -34,7 +37,7 @@
 
 #include "ref_luts.h"
 
-enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4 };
+enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4, ORC_I32 = 5 };
 enum { ORC_MC = 0, ORC_MT = 1, ORC_NSN = 2 };
 enum { ORC_OK = 0, ORC_EINVAL = 1, ORC_ENOMEM = 2 };
 
@@ -79,23 +82,62 @@ static int out_type(const int *tys, int n) {
     return ORC_F64; /* float(Integer) == Float64 */
 }
 
+static int is_wide_int(int ty) { return ty == ORC_I32 || ty == ORC_I64; }
+static double pun(int64_t i) {
+    double d;
+    memcpy(&d, &i, sizeof d);
+    return d;
+}
+static int64_t unpun(double d) {
+    int64_t i;
+    memcpy(&i, &d, sizeof i);
+    return i;
+}
+
 static double load(const orc_ctx *c, int64_t x, int64_t y, int64_t z) {
     int64_t i = x + c->nx * (y + c->ny * z);
     switch (c->T) {
     case ORC_U16: return (double)((const uint16_t *)c->vol)[i];
     case ORC_F32: return (double)((const float *)c->vol)[i];
+    case ORC_I32: return pun((int64_t)((const int32_t *)c->vol)[i]);
+    case ORC_I64: return pun(((const int64_t *)c->vol)[i]);
     default: return ((const double *)c->vol)[i];
     }
 }
 
-/* `iso_vals[k] < iso` (src/common.jl:11-18): Julia compares mixed types exactly;
- * every supported value is exact in double. */
-static int below(const orc_ctx *c, double v) { return v < c->iso; }
+/* `iso_vals[k] < iso` (src/common.jl:11-18): Julia compares mixed types exactly.
+ * UInt16 and float values are exact in double; an Int32 / Int64 value x is
+ * compared with the (integral or float) iso as x < ceil(iso). */
+static int below(const orc_ctx *c, double v) {
+    if (!is_wide_int(c->T)) return v < c->iso;
+    const int64_t x = unpun(v);
+    if (isnan(c->iso)) return 0;
+    const double t = ceil(c->iso);
+    if (t >= 9223372036854775808.0) return 1;   /* beyond every Int64 */
+    if (t < -9223372036854775808.0) return 0;
+    return x < (int64_t)t;
+}
 
 /* (iso - v1) / (v2 - v1) in Julia's promoted arithmetic (src/marching_cubes.jl:101,
  * src/marching_tetrahedra.jl:48). */
 static double quotient(const orc_ctx *c, double v1, double v2) {
     double den;
+    if (is_wide_int(c->T)) {
+        const int64_t a = unpun(v1), b = unpun(v2);
+        /* v2 - v1 in the data type, wrapping */
+        const int64_t d = c->T == ORC_I32 ? (int64_t)(int32_t)((uint32_t)b - (uint32_t)a)
+                                          : (int64_t)((uint64_t)b - (uint64_t)a);
+        if (c->Q == ORC_F32) {  /* Float32 iso: Float32(iso) - Float32(v1), Float32(v2 - v1) */
+            const double num = rnd(ORC_F32, (double)(float)c->isoq - (double)(float)a);
+            return rnd(ORC_F32, num / (double)(float)d);
+        }
+        if (c->I == ORC_I64) {  /* Int64 iso: (iso - v1) in Int64 (wrapping for Int64 data), then Int / Int */
+            const int64_t n = c->T == ORC_I64 ? (int64_t)((uint64_t)(int64_t)c->iso - (uint64_t)a)
+                                              : (int64_t)c->iso - a;
+            return (double)n / (double)d;
+        }
+        return (c->isoq - (double)a) / (double)d;  /* Float64 iso */
+    }
     if (c->T == ORC_U16)
         den = (double)(uint16_t)((uint16_t)v2 - (uint16_t)v1); /* UInt16 wraps */
     else if (c->T == ORC_F32)
@@ -419,7 +461,7 @@ static int run_nsn(const orc_ctx *c, orc_mesh *m) {
 static int setup(orc_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int alg, int I, double iso,
                  int E, double eps, int R, const double *rg) {
     memset(c, 0, sizeof(*c));
-    if (T != ORC_U16 && T != ORC_F32 && T != ORC_F64) return ORC_EINVAL;
+    if (T != ORC_U16 && T != ORC_F32 && T != ORC_F64 && T != ORC_I32 && T != ORC_I64) return ORC_EINVAL;
     if (I != ORC_F32 && I != ORC_F64 && I != ORC_I64) return ORC_EINVAL;
     if (R != ORC_F32 && R != ORC_F64 && R != ORC_I64) return ORC_EINVAL;
     if (alg == ORC_MT && E != ORC_F32 && E != ORC_F64) return ORC_EINVAL;
@@ -427,7 +469,8 @@ static int setup(orc_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int
     c->T = T; c->I = I; c->E = E; c->R = R;
     c->vol = vol; c->nx = nx; c->ny = ny; c->nz = nz;
     c->iso = iso;
-    int q64 = (T == ORC_F64) || (I == ORC_F64) || (T == ORC_U16 && I == ORC_I64);
+    /* promote(typeof(iso), T) for the quotient; Int / Int divides in Float64 */
+    int q64 = (T == ORC_F64) || (I == ORC_F64) || (T != ORC_F32 && I == ORC_I64);
     c->Q = q64 ? ORC_F64 : ORC_F32;
     c->isoq = rnd(c->Q, iso);
     c->L = (R == ORC_F32) ? ORC_F32 : ORC_F64;

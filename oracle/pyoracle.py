@@ -46,7 +46,12 @@ def _promote(*tys):
         return np.float32
     if np.int64 in tys:
         return np.int64
+    if np.int32 in tys:
+        return np.int32
     return np.uint16
+
+
+_INTS = (np.uint16, np.int32, np.int64)
 
 
 def _float(t):
@@ -63,7 +68,7 @@ def _linrange(a, b, n):
 
 
 def _sub(T, a, b):
-    """a - b in the promoted type of (T, T) -- UInt16 wraps."""
+    """a - b in the promoted type of (T, T) -- machine integers wrap."""
     with np.errstate(over='ignore'):
         return T(a) - T(b)
 
@@ -73,14 +78,15 @@ def _quot(iso, v1, v2):
     T = type(v1)
     I = _jl_type(iso)
     den = _sub(T, v2, v1)
-    if T is np.uint16 and I is np.int64:
-        return np.float64(np.int64(iso) - np.int64(v1)) / np.float64(den)
+    if T in _INTS and I is np.int64:
+        # Int / Int: the integer difference (wrapping in Int64), then Float64 division
+        return np.float64(_sub(np.int64, np.int64(iso), v1)) / np.float64(den)
     num_t = _promote(T, I)
-    if num_t is np.int64:
+    if num_t in _INTS:
         num_t = np.float64
     num = num_t(iso) - num_t(v1)
     q_t = _promote(type(num), type(den))
-    if q_t in (np.int64, np.uint16):
+    if q_t in _INTS:
         q_t = np.float64
     return q_t(num) / q_t(den)
 
@@ -118,13 +124,16 @@ def isosurface(vol, alg='mc', iso=0.0, eps=1e-3, ranges=((-1, 1), (-1, 1), (-1, 
     R = _jl_type(ranges[0][0])
     tys = [R, T, _jl_type(iso)] + ([_jl_type(eps)] if alg == 'mt' else [])
     FT = _promote(*tys)
-    O = _float(FT) if FT is not np.int64 and FT is not np.uint16 else np.float64
+    O = _float(FT) if FT not in _INTS else np.float64
     xp, L = _linrange(ranges[0][0], ranges[0][1], nx)
     yp, _ = _linrange(ranges[1][0], ranges[1][1], ny)
     zp, _ = _linrange(ranges[2][0], ranges[2][1], nz)
     verts, faces = [], []
 
     def below(v):
+        # exact mixed comparison, as Julia's `<` (Python compares int and float exactly)
+        if T in _INTS:
+            return int(v) < (iso if isinstance(iso, (int, np.integer)) else float(iso))
         return float(v) < float(iso)
 
     if alg == 'mc':

@@ -216,3 +216,32 @@ def test_fill_without_count_is_rejected(pkg, cuda):
     c = pkg.Context(0)
     rc = pkg.load_library().mesh_fill(c.handle, None, None, 0)
     assert rc == 5  # MESH_ESTATE
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+@pytest.mark.parametrize('dt', [np.int32, np.int64])
+def test_integer_volumes(pkg, oracle, cuda, alg, dt):
+    # test/runtests.jl:66-75 runs every algorithm on rand(Int, 10, 10, 10): exact
+    # integer-vs-iso comparison, v2 - v1 wrapping in the data type, the quotient in
+    # promote(typeof(iso), T) (Int / Int divides in Float64); output Float64 by default
+    rng = np.random.default_rng(int(np.dtype(dt).itemsize) + len(alg))
+    info = np.iinfo(dt)
+    A = rng.integers(info.min, info.max, (10, 10, 10), dtype=dt, endpoint=True)
+    v, f = check(pkg, oracle, A, alg)
+    assert v.dtype == np.float64 and f.dtype == np.int64
+    for trial in range(3):
+        shape = tuple(int(s) for s in rng.integers(2, 20, 3))
+        full = rng.integers(info.min, info.max, shape, dtype=dt, endpoint=True)
+        small = rng.integers(-1000, 1000, shape).astype(dt)
+        for B, isos in ((full, [0.0, np.float32(1e9), 0, -123456789]), (small, [0.5, np.float32(-3.25), 7])):
+            for iso in isos:
+                check(pkg, oracle, B, alg, iso, np.float32(1e-3) if isinstance(iso, np.float32) else 1e-3)
+                check(pkg, oracle, B, alg, iso, 1e-3, ((np.float32(-2), np.float32(3)),) * 3, device=True)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_integer_field_many_tiles(pkg, oracle, cuda, alg):
+    # a smooth Int32 field over several x tiles, y tiles and z segments
+    A = (sphere(0, 0.6, np.float64, c=(0.1, 0.0, -0.05), shape=(97, 70, 133)) * 100000).astype(np.int32)
+    check(pkg, oracle, A, alg, 0)
+    check(pkg, oracle, A, alg, 2500.5, 1e-3, ((0, 1),) * 3, device=True)

@@ -150,3 +150,39 @@ def test_uint16_wraparound_is_reproduced(oracle):
     mu = (500 - 900) / float((0 - 900) % 65536)
     assert len(v) == 3 and len(f) == 1
     assert np.isclose(v[0, 0], -1 + mu * 2)  # edge 1 runs along +x from x=-1
+
+
+@pytest.mark.parametrize('dt', [np.int32, np.int64])
+def test_integer_volumes_c_matches_python(oracle, dt):
+    # Int32 / Int64 volumes (test/runtests.jl:66-75 runs every algorithm on rand(Int, ...)):
+    # exact integer-vs-iso comparison, v2 - v1 wrapping in the data type, and the
+    # quotient in promote(typeof(iso), T) -- Int / Int divides in Float64
+    rng = np.random.default_rng(int(np.dtype(dt).itemsize))
+    info = np.iinfo(dt)
+    for trial in range(5):
+        sh = tuple(int(s) for s in rng.integers(2, 7, 3))
+        full = rng.integers(info.min, info.max, sh, dtype=dt, endpoint=True)  # wrapping differences
+        small = rng.integers(-1000, 1000, sh).astype(dt)
+        for A, isos in ((full, [0.0, np.float32(1e9), 0, -123456789]), (small, [0.5, np.float32(-3.25), 7, 0.0])):
+            A = np.asfortranarray(A)
+            for iso in isos:
+                for alg in ('mc', 'mt', 'nsn'):
+                    for rg in (((-1, 1),) * 3, ((np.float32(-2), np.float32(3)),) * 3):
+                        a = oracle.isosurface(A, alg, iso, 1e-3, rg)
+                        b = pyoracle.isosurface(A, alg, iso, 1e-3, rg) if alg != 'nsn' else a
+                        assert a[0].dtype == b[0].dtype
+                        assert np.array_equal(a[1], b[1]), (dt, iso, alg)
+                        assert np.array_equal(a[0], b[0], equal_nan=True), (dt, iso, alg)
+
+
+@pytest.mark.parametrize('dtype,iso,rt,bits', [
+    (np.int64, 0.0, 4, 64),            # test/runtests.jl:66-75: rand(Int) data, default iso -> Float64
+    (np.int32, 0.0, 4, 64),
+    (np.int64, np.float32(0), 4, 32),  # promote(Int64, Float32) == Float32
+    (np.int64, 0, 4, 64),              # float(Int64) == Float64
+    (np.int32, 0, 2, 32),
+])
+def test_integer_volume_eltype_rule(oracle, dtype, iso, rt, bits):
+    for alg in ('mc', 'mt'):
+        eps = np.float32(1e-3) if bits == 32 else 1e-3
+        assert oracle.output_bits(dtype, alg, iso, eps, rt) == bits
