@@ -507,6 +507,59 @@ def run_serving(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_ct(args, rank, world):
+    """MarchingCubes(iso=500) on the UInt16 512^3 CT-like volume: background
+    N(100, 20) clamped to >= 0 plus 3 seeded ellipsoidal shells N(1000, 50), 4
+    voxels thick (X = Y = Z = -1:1; UInt16 differences wrap).  Device time per
+    call through mesh_extract_device, per stage, and the roofline of each kernel."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    import meshing_gb300.fields as fields
+    n = args.n if args.n != N_DEFAULT else 512
+    t = fields.ct_like_u16(n, seed=SEED)
+    torch.cuda.synchronize()
+    m = pkg.MarchingCubes(iso=500)
+    ctx = pkg.Context(0)
+    v, f = pkg.isosurface(t, m, ctx=ctx)
+    verts, faces = torch.empty_like(v), torch.empty_like(f)
+    for _ in range(args.warmup):
+        pkg.isosurface_device(t, m, verts=verts, faces=faces, ctx=ctx)
+    ctx.sync()
+    ctx.stage_times()
+    ctx.enable_timing(True)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        pkg.isosurface_device(t, m, verts=verts, faces=faces, ctx=ctx)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    st = {k: v_[0] / max(v_[1], 1) for k, v_ in ctx.stage_times().items() if v_[1]}
+    ok = torch.equal(verts, v) and torch.equal(faces, f)
+    ctx.close()
+    peak, peak_kind = measured_peak()
+    in_b = float(n) ** 3 * 2
+    out_b = v.shape[0] * 24 + f.shape[0] * 24  # Float64 vertices (Int ranges, Int iso)
+    kern = {'classify': (st.get('classify', 0), in_b), 'compact': (st.get('emit', 0), in_b),
+            'expand': (st.get('expand', 0), out_b)}
+    roof = {k: {'ms': t_, 'gbs': b / (t_ * 1e-3) / 1e9 if t_ else None,
+                'frac': b / (t_ * 1e-3) / 1e9 / peak if t_ else None} for k, (t_, b) in kern.items()}
+    if rank == 0:
+        print(json.dumps({'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes', 'workload': 'ct',
+                          'value': n ** 3 / (ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': ms,
+                          'dtype': 'u16', 'data': 'synthetic',
+                          'config': {'workload': 'UInt16 %d^3 CT-like volume (N(100,20) background, 3 seeded '
+                                                 'ellipsoidal shells N(1000,50)), MarchingCubes(iso=500)' % n,
+                                     'nverts': v.shape[0], 'nfaces': f.shape[0], 'output': 'Float64 vertices',
+                                     'stage_ms': st, 'repeatable': bool(ok)},
+                          'kernels': roof, 'peak': peak, 'peak_source': peak_kind,
+                          'pipeline': {'bytes': in_b + out_b, 'frac': (in_b + out_b) / (ms * 1e-3) / 1e9 / peak}}),
+              flush=True)
+
+
 def run_gyroid(args, rank, world):
     """MarchingCubes, MarchingTetrahedra and NaiveSurfaceNets, iso 0, on the
     Float32 gyroid sin x cos y + sin y cos z + sin z cos x over [-3pi, 3pi]^3
@@ -560,7 +613,7 @@ def main():
     ap.add_argument('--cpu-planes', type=int, default=None,
                     help='z cell planes of the CPU sample (default 600, about 12 s on one core; 32 per step for --impl reference)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
-    ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving', 'gyroid'],
+    ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving', 'gyroid', 'ct'],
                     help='plain: one 1024^3 volume (the headline); batched: many uneven volumes; serving: the '
                          'serving loop under Poisson arrivals')
     ap.add_argument('--volumes', type=int, default=4096, help='volumes of the batched workload')
@@ -592,6 +645,8 @@ def main():
             run_serving(args, rank, world)
         elif args.workload == 'gyroid':
             run_gyroid(args, rank, world)
+        elif args.workload == 'ct':
+            run_ct(args, rank, world)
         else:
             run_ours(args, rank, world, dist)
     finally:

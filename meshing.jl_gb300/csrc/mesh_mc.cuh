@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
                 const BatchVol &b = p.bvols[sm.vol[j]];
                 out -= p.vol_off[2 * sm.vol[j]];
                 vout = b.verts;
-                if (out >= b.vcap) {
+                if (out < 0 || out >= b.vcap) {
                     atomicOr(p.err, ERR_CAPACITY);
                     continue;
                 }
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
             if (MODE == EXP_BATCH && p.vol_outputs) {
                 const BatchVol &b = p.bvols[sm.vol[j]];
                 const int64_t lf = sm.fb[j] + k - p.vol_off[2 * sm.vol[j] + 1];
-                if (lf >= b.fcap) {
+                if (lf < 0 || lf >= b.fcap) {
                     atomicOr(p.err, ERR_CAPACITY);
                     continue;
                 }

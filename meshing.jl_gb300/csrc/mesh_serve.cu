@@ -150,6 +150,7 @@ struct Slot {
     cudaStream_t stream = nullptr;
     mesh_ctx *ctx = nullptr;       // Marching Tetrahedra / Naive Surface Nets requests
     int busy = 0;
+    int launching = 0;             // the loop thread is queuing this slot's wave
     char *stage = nullptr;         // pinned staging of batch plans
     size_t stage_cap = 0;
     int64_t *res = nullptr;        // pinned results: counts and error words
@@ -159,6 +160,17 @@ struct Slot {
     std::vector<Group> groups;
     std::vector<int64_t> singles;  // single-volume requests of the wave
     size_t single_res_off = 0;
+    // copies of the wave's requests, taken under the lock at admission: the
+    // launch reads these, never the server's request map, which other threads
+    // grow (and rehash) while a wave is being queued
+    std::unordered_map<int64_t, Req> wave;
+    uint64_t seq = 0;  // waves launched on this slot
+};
+
+// Argument of a wave's host function: the slot and which of its waves.
+struct WaveTag {
+    Slot *sl;
+    uint64_t seq;
 };
 
 // Scratch of a Marching Cubes batch laid out in one block.
@@ -282,6 +294,7 @@ bool same_key(const Group &g, const Req &r) {
 void form_wave(mesh_server *s, Slot &sl) {
     sl.groups.clear();
     sl.singles.clear();
+    sl.wave.clear();
     int admitted = 0;
     while (!s->queue.empty() && admitted < s->max_wave) {
         Req &r = s->reqs[s->queue.front()];
@@ -324,6 +337,7 @@ void form_wave(mesh_server *s, Slot &sl) {
         }
         s->queue.pop_front();
         r.state = RQ_RUNNING;
+        sl.wave[r.id] = r;
         admitted++;
     }
     // scratch blocks; if first-fit cannot place one, hand that batch's requests back
@@ -337,6 +351,7 @@ void form_wave(mesh_server *s, Slot &sl) {
             s->pool.release(&r.out);
             r.state = RQ_QUEUED;
             s->queue.push_front(*it);
+            sl.wave.erase(*it);
         }
         sl.groups.erase(sl.groups.begin() + g);
     }
@@ -344,10 +359,14 @@ void form_wave(mesh_server *s, Slot &sl) {
 
 // Host function queued after a wave: publish results, free the wave's scratch.
 void CUDART_CB wave_done(void *arg) {
-    Slot *sl = (Slot *)arg;
+    WaveTag *tag = (WaveTag *)arg;
+    Slot *sl = tag->sl;
+    const uint64_t seq = tag->seq;
+    delete tag;
     mesh_server *s = sl->srv;
     const clk::time_point now = clk::now();
     std::lock_guard<std::mutex> lk(s->mu);
+    if (seq != sl->seq || !sl->busy) return;  // this wave was already failed
     auto finish = [&](Req &r, int64_t nv, int64_t nf, unsigned err) {
         r.t_done = now;
         if (err) {
@@ -384,6 +403,7 @@ void CUDART_CB wave_done(void *arg) {
     }
     sl->groups.clear();
     sl->singles.clear();
+    sl->wave.clear();
     sl->busy = 0;
     s->cv.notify_all();
 }
@@ -424,7 +444,7 @@ int launch_wave(mesh_server *s, Slot &sl) {
     size_t stage = 0;
     for (size_t gi = 0; gi < sl.groups.size(); gi++) {
         std::vector<const Req *> rs;
-        for (int64_t id : sl.groups[gi].reqs) rs.push_back(&s->reqs[id]);
+        for (int64_t id : sl.groups[gi].reqs) rs.push_back(&sl.wave.at(id));
         layout_group(rs, &lays[gi]);
         if (lays[gi].total > sl.groups[gi].scratch.size) return MESH_EDEVICE;  // bound violated: never launch
         sl.groups[gi].stage_off = stage;
@@ -439,7 +459,7 @@ int launch_wave(mesh_server *s, Slot &sl) {
         Group &g = sl.groups[gi];
         GroupLayout &L = lays[gi];
         std::vector<const Req *> rs;
-        for (int64_t id : g.reqs) rs.push_back(&s->reqs[id]);
+        for (int64_t id : g.reqs) rs.push_back(&sl.wave.at(id));
         char *blk = s->arena + g.scratch.off;
         const int n = (int)rs.size();
         Plan P{};
@@ -525,7 +545,7 @@ int launch_wave(mesh_server *s, Slot &sl) {
         }
         if ((e = cudaMemsetAsync(sl.d_counts, 0, need, sl.stream)) != cudaSuccess) return MESH_ECUDA;
         for (size_t i = 0; i < sl.singles.size(); i++) {
-            Req &r = s->reqs[sl.singles[i]];
+            const Req &r = sl.wave.at(sl.singles[i]);
             int rc = mesh_extract_device(sl.ctx, r.vol, r.T, r.dims[0], r.dims[1], r.dims[2], &r.p,
                                          s->arena + r.out.off, r.vcap, (int64_t *)(s->arena + r.out.off + r.vbytes),
                                          r.fcap, sl.d_counts + 3 * i);
@@ -540,8 +560,36 @@ int launch_wave(mesh_server *s, Slot &sl) {
             cudaSuccess)
             return MESH_ECUDA;
     }
-    e = cudaLaunchHostFunc(sl.stream, wave_done, &sl);
+    WaveTag *tag = new (std::nothrow) WaveTag{&sl, sl.seq};
+    if (!tag) return MESH_ENOMEM;
+    e = cudaLaunchHostFunc(sl.stream, wave_done, tag);
+    if (e != cudaSuccess) delete tag;
     return e == cudaSuccess ? MESH_OK : MESH_ECUDA;
+}
+
+// Fails the requests of a wave that will not complete, frees its scratch and
+// the slot.  Called with the lock held.
+void fail_wave(mesh_server *s, Slot &sl, int rc) {
+    for (auto &g : sl.groups) {
+        for (int64_t id : g.reqs) {
+            Req &r = s->reqs[id];
+            r.state = RQ_FAILED;
+            r.status = rc;
+            s->failed++;
+        }
+        s->pool.release(&g.scratch);
+    }
+    for (int64_t id : sl.singles) {
+        Req &r = s->reqs[id];
+        r.state = RQ_FAILED;
+        r.status = rc;
+        s->failed++;
+    }
+    sl.groups.clear();
+    sl.singles.clear();
+    sl.wave.clear();
+    sl.busy = 0;
+    s->cv.notify_all();
 }
 
 void loop(mesh_server *s) {
@@ -553,44 +601,45 @@ void loop(mesh_server *s) {
                 if (!sl.busy) return &sl;
             return (Slot *)nullptr;
         };
-        s->cv.wait(lk, [&] { return s->stop || (!s->queue.empty() && free_slot()); });
+        // a wave whose stream reports an error never reaches wave_done: fail it
+        auto reap = [&]() {
+            for (auto &sl : s->slots) {
+                if (!sl.busy || sl.launching) continue;
+                const cudaError_t e = cudaStreamQuery(sl.stream);
+                if (e != cudaSuccess && e != cudaErrorNotReady) {
+                    s->msg = std::string("wave failed on the device: ") + cudaGetErrorString(e);
+                    fail_wave(s, sl, MESH_ECUDA);
+                }
+            }
+        };
+        while (!s->cv.wait_for(lk, std::chrono::milliseconds(50),
+                               [&] { return s->stop || (!s->queue.empty() && free_slot()); }))
+            reap();
         if (s->stop) break;
         Slot &sl = *free_slot();
         form_wave(s, sl);
         if (sl.groups.empty() && sl.singles.empty()) {
             // the head does not fit now: wait for a wave to finish or a release
-            s->cv.wait(lk);
+            s->cv.wait_for(lk, std::chrono::milliseconds(50));
+            reap();
             continue;
         }
         sl.busy = 1;
+        sl.launching = 1;
+        sl.seq++;
         s->waves++;
         for (auto &g : sl.groups) s->wave_reqs += (int64_t)g.reqs.size();
         s->wave_reqs += (int64_t)sl.singles.size();
         lk.unlock();
         const int rc = launch_wave(s, sl);
         lk.lock();
+        sl.launching = 0;
         if (rc) {  // nothing of this wave will complete: fail its requests
             s->msg = "wave launch failed";
+            lk.unlock();
             cudaStreamSynchronize(sl.stream);
-            for (auto &g : sl.groups) {
-                for (int64_t id : g.reqs) {
-                    Req &r = s->reqs[id];
-                    r.state = RQ_FAILED;
-                    r.status = rc;
-                    s->failed++;
-                }
-                s->pool.release(&g.scratch);
-            }
-            for (int64_t id : sl.singles) {
-                Req &r = s->reqs[id];
-                r.state = RQ_FAILED;
-                r.status = rc;
-                s->failed++;
-            }
-            sl.groups.clear();
-            sl.singles.clear();
-            sl.busy = 0;
-            s->cv.notify_all();
+            lk.lock();
+            fail_wave(s, sl, rc);
         }
     }
 }

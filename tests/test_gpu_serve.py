@@ -108,3 +108,35 @@ def test_empty_and_degenerate_requests(pkg, cuda):
             assert v.shape[0] == 0 and f.shape[0] == 0
             srv.release(rid)
     srv.close()
+
+
+def test_bursts_and_concurrent_submitters(pkg, cuda):
+    # many requests submitted at once and from several threads while waves are
+    # being launched (the server's request map grows while waves are queued)
+    torch = cuda
+    import threading
+    import meshing_gb300.fields as fields
+    rng = np.random.default_rng(21)
+    vols = [fields.primitives_sdf((48, 40, 56), fields.primitives_params(rng)) for _ in range(8)]
+    m = pkg.MarchingCubes(iso=np.float32(0))
+    want = [pkg.isosurface(v, m) for v in vols]
+    srv = pkg.Server(budget_bytes=8 << 30, slots=3, max_wave=64)
+    srv.replay([(vols[i % 8], m, ((-1, 1),) * 3) for i in range(512)], np.zeros(512))
+    st = srv.stats()
+    assert st['completed'] == 512 and st['failed'] == 0
+    ids = [[] for _ in range(4)]
+
+    def submit(k):
+        for i in range(120):
+            ids[k].append((i % 8, srv.submit(vols[i % 8], m)))
+
+    th = [threading.Thread(target=submit, args=(k,)) for k in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for lst in ids:
+        for i, rid in lst:
+            assert same(torch, srv.result(rid), want[i])
+            srv.release(rid)
+    srv.close()
