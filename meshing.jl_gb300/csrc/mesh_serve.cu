@@ -839,9 +839,9 @@ int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int
             }
             if (id <= 0) continue;
             int st = 0, tries = 0;
-            // a request that has not ended after 600 s is reported, not waited for
+            // a request that has not ended after 120 s is reported, not waited for
             while (mesh_server_wait(s, id, 1000000, &st, nullptr, nullptr, nullptr, nullptr) == MESH_OK &&
-                   st != RQ_DONE && ++tries < 600)
+                   st != RQ_DONE && ++tries < 120)
                 ;
             if (st == RQ_QUEUED || st == RQ_RUNNING) {
                 std::lock_guard<std::mutex> lk(m);
@@ -873,7 +873,7 @@ int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int
         cv.notify_all();
     }
     rel.join();
-    return stuck ? sfail(s, MESH_EDEVICE, "a replayed request did not end within 600 s") : MESH_OK;
+    return stuck ? sfail(s, MESH_EDEVICE, "a replayed request did not end within 120 s") : MESH_OK;
 }
 
 int mesh_server_reset_stats(mesh_server *s) {
