@@ -80,6 +80,23 @@ struct Pool {
         }
         return false;
     }
+    // The same from the top of the highest free chunk that fits (finished meshes
+    // are kept there, away from the worst-case blocks of requests in flight).
+    bool alloc_top(size_t n, Block *b) {
+        n = up(std::max<size_t>(n, 1));
+        for (auto it = free_.rbegin(); it != free_.rend(); ++it) {
+            if (it->second < n) continue;
+            const size_t o = it->first, sz = it->second;
+            free_.erase(std::next(it).base());
+            if (sz > n) free_[o] = sz - n;
+            b->off = o + sz - n;
+            b->size = n;
+            used += n;
+            peak = std::max(peak, used);
+            return true;
+        }
+        return false;
+    }
     // Frees [o, o + n) of an allocated block (both multiples of GRAIN).
     void release_range(size_t o, size_t n) {
         if (!n) return;
@@ -126,8 +143,9 @@ struct Req {
     int out64 = 0;
     int64_t vcap = 0, fcap = 0;
     size_t vbytes = 0;  // bytes of the vertex part of the output block
-    Block out;          // worst case while queued / running: vertices at 0, faces at vbytes
-    Block keep_v, keep_f;  // after completion: the parts of `out` that hold the mesh
+    Block out;          // worst case while in flight: vertices at 0, faces at vbytes
+    Block keep_v, keep_f;  // after completion: the blocks holding the mesh
+    Block move_v, move_f;  // while the mesh is being moved: where it goes
     int state = RQ_QUEUED;
     int status = MESH_OK;
     int64_t nverts = 0, nfaces = 0;
@@ -165,6 +183,7 @@ struct Slot {
     // grow (and rehash) while a wave is being queued
     std::unordered_map<int64_t, Req> wave;
     uint64_t seq = 0;  // waves launched on this slot
+    int finishing = 0; // the wave's kernels are done; its meshes still have to be moved
 };
 
 // Argument of a wave's host function: the slot and which of its waves.
@@ -290,14 +309,22 @@ bool same_key(const Group &g, const Req &r) {
 }
 
 // Takes queued requests into slot `sl` while their outputs and the batches'
-// scratch fit the pool.  Called with the lock held.
+// scratch fit the pool.  A wave reserves at most its slot's share of the pool
+// (beyond its first request): one wave taking all the memory of a backlog would
+// leave the other slots idle and the device running one wave at a time.
+// Called with the lock held.
 void form_wave(mesh_server *s, Slot &sl) {
     sl.groups.clear();
     sl.singles.clear();
     sl.wave.clear();
     int admitted = 0;
+    const size_t share_cap = s->pool.cap / s->slots.size();
+    size_t reserved = 0;
     while (!s->queue.empty() && admitted < s->max_wave) {
         Req &r = s->reqs[s->queue.front()];
+        const size_t est = out_bytes(r) + (r.p.alg == MESH_ALG_MC ? vol_scratch_bytes(r) : 0);
+        if (admitted && reserved + est > share_cap) break;
+        reserved += est;
         int gi = -1;
         if (r.p.alg == MESH_ALG_MC) {
             for (size_t g = 0; g < sl.groups.size(); g++)
@@ -357,7 +384,64 @@ void form_wave(mesh_server *s, Slot &sl) {
     }
 }
 
-// Host function queued after a wave: publish results, free the wave's scratch.
+// Fails the requests of a wave that will not complete, frees its scratch and
+// the slot.  Called with the lock held.
+void fail_wave(mesh_server *s, Slot &sl, int rc) {
+    for (auto &g : sl.groups) {
+        for (int64_t id : g.reqs) {
+            Req &r = s->reqs[id];
+            r.state = RQ_FAILED;
+            r.status = rc;
+            s->failed++;
+        }
+        s->pool.release(&g.scratch);
+    }
+    for (int64_t id : sl.singles) {
+        Req &r = s->reqs[id];
+        r.state = RQ_FAILED;
+        r.status = rc;
+        s->failed++;
+    }
+    sl.groups.clear();
+    sl.singles.clear();
+    sl.wave.clear();
+    sl.finishing = 0;
+    sl.busy = 0;
+    s->cv.notify_all();
+}
+
+// Publishes the results of slot sl's wave and frees the slot.  Lock held.
+void complete_wave(mesh_server *s, Slot &sl, clk::time_point now) {
+    auto finish = [&](int64_t id) {
+        Req &r = s->reqs[id];
+        r.t_done = now;
+        if (r.status) {
+            r.state = RQ_FAILED;
+            s->failed++;
+            return;
+        }
+        r.state = RQ_DONE;
+        s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_sub).count());
+        s->samples += (double)r.dims[0] * r.dims[1] * r.dims[2];
+        s->t_last = now;
+    };
+    for (auto &g : sl.groups)
+        for (int64_t id : g.reqs) finish(id);
+    for (int64_t id : sl.singles) finish(id);
+    sl.groups.clear();
+    sl.singles.clear();
+    sl.wave.clear();
+    sl.finishing = 0;
+    sl.busy = 0;
+    s->cv.notify_all();
+}
+
+// Host function queued after a wave's kernels.  Each finished mesh keeps the
+// start of its worst-case block and frees the rest, and the wave's scratch is
+// freed.  Held meshes left where the worst-case blocks were can split the free
+// space into holes too small for the next worst case (the queue's head, or one
+// like this wave's): then the loop thread first moves them to the top of the
+// pool (finish_wave); otherwise the wave is complete.
 void CUDART_CB wave_done(void *arg) {
     WaveTag *tag = (WaveTag *)arg;
     Slot *sl = tag->sl;
@@ -367,45 +451,116 @@ void CUDART_CB wave_done(void *arg) {
     const clk::time_point now = clk::now();
     std::lock_guard<std::mutex> lk(s->mu);
     if (seq != sl->seq || !sl->busy) return;  // this wave was already failed
-    auto finish = [&](Req &r, int64_t nv, int64_t nf, unsigned err) {
-        r.t_done = now;
-        if (err) {
-            r.state = RQ_FAILED;
+    size_t room = 0;  // the largest worst case of the wave
+    auto record = [&](Req &r, int64_t nv, int64_t nf, unsigned err) {
+        room = std::max(room, r.out.size);
+        if (err) {  // the worst-case block stays reserved until the release
             r.status = (err & ERR_CAPACITY) ? MESH_ECAPACITY : MESH_EDEVICE;
-            s->failed++;
-        } else {
-            r.state = RQ_DONE;
-            r.nverts = nv;
-            r.nfaces = nf;
-            // keep only the mesh: the rest of the worst-case block goes back to the pool
-            const size_t vb = up((size_t)nv * 3 * (r.out64 ? 8 : 4)), fb = up((size_t)nf * 24);
-            r.keep_v = Block{r.out.off, vb};
-            r.keep_f = Block{r.out.off + r.vbytes, fb};
-            s->pool.release_range(r.out.off + vb, r.vbytes - vb);
-            s->pool.release_range(r.out.off + r.vbytes + fb, r.out.size - r.vbytes - fb);
-            r.out.size = 0;
-            s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_sub).count());
-            s->samples += (double)r.dims[0] * r.dims[1] * r.dims[2];
+            return;
         }
-        s->t_last = now;
+        r.nverts = nv;
+        r.nfaces = nf;
+        const size_t vb = up((size_t)nv * 3 * (r.out64 ? 8 : 4)), fb = up((size_t)nf * 24);
+        r.keep_v = Block{r.out.off, vb};
+        r.keep_f = Block{r.out.off + r.vbytes, fb};
+        s->pool.release_range(r.out.off + vb, r.vbytes - vb);
+        s->pool.release_range(r.out.off + r.vbytes + fb, r.out.size - r.vbytes - fb);
+        r.out.size = 0;
     };
     for (auto &g : sl->groups) {
         const int64_t *o = sl->res + g.res_off;  // offsets [n+1][2], then the error word
         const size_t n = g.reqs.size();
         const unsigned err = (unsigned)(o[2 * (n + 1)] & 0xffffffffll);
         for (size_t i = 0; i < n; i++)
-            finish(s->reqs[g.reqs[i]], o[2 * i + 2] - o[2 * i], o[2 * i + 3] - o[2 * i + 1], err);
+            record(s->reqs[g.reqs[i]], o[2 * i + 2] - o[2 * i], o[2 * i + 3] - o[2 * i + 1], err);
         s->pool.release(&g.scratch);
     }
     for (size_t i = 0; i < sl->singles.size(); i++) {
         const int64_t *o = sl->res + sl->single_res_off + 3 * i;
-        finish(s->reqs[sl->singles[i]], o[0], o[1], (unsigned)(o[2] & 0xffffffffll));
+        record(s->reqs[sl->singles[i]], o[0], o[1], (unsigned)(o[2] & 0xffffffffll));
     }
-    sl->groups.clear();
-    sl->singles.clear();
-    sl->wave.clear();
-    sl->busy = 0;
-    s->cv.notify_all();
+    if (!s->queue.empty()) {
+        const Req &h = s->reqs[s->queue.front()];
+        room = std::max(room, out_bytes(h) + (h.p.alg == MESH_ALG_MC ? vol_scratch_bytes(h) : 0));
+    }
+    if (s->pool.largest() < room) {
+        sl->finishing = 1;
+        s->cv.notify_all();
+        return;
+    }
+    complete_wave(s, *sl, now);
+}
+
+// Host function queued after the mesh moves: the meshes are in their new
+// blocks, the old ones are freed and the wave is complete.
+void CUDART_CB moves_done(void *arg) {
+    WaveTag *tag = (WaveTag *)arg;
+    Slot *sl = tag->sl;
+    const uint64_t seq = tag->seq;
+    delete tag;
+    mesh_server *s = sl->srv;
+    const clk::time_point now = clk::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (seq != sl->seq || !sl->busy) return;
+    auto settle = [&](int64_t id) {
+        Req &r = s->reqs[id];
+        if (!r.move_v.size && !r.move_f.size) return;
+        s->pool.release(&r.keep_v);
+        s->pool.release(&r.keep_f);
+        r.keep_v = r.move_v;
+        r.keep_f = r.move_f;
+        r.move_v.size = r.move_f.size = 0;
+    };
+    for (auto &g : sl->groups)
+        for (int64_t id : g.reqs) settle(id);
+    for (int64_t id : sl->singles) settle(id);
+    complete_wave(s, *sl, now);
+}
+
+// Moves every finished mesh of slot sl into blocks at the top of the pool
+// (leaving a mesh in place when they do not fit), then queues moves_done.
+// Called with the lock held; unlocks around the CUDA calls.
+void finish_wave(mesh_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
+    sl.finishing = 0;
+    struct Move {
+        size_t src, dst, bytes;
+    };
+    std::vector<Move> moves;
+    auto plan = [&](int64_t id) {
+        Req &r = s->reqs[id];
+        const size_t vb = r.keep_v.size, fb = r.keep_f.size;
+        if (r.status || (!vb && !fb)) return;
+        Block bv, bf;
+        if (vb && !s->pool.alloc_top(vb, &bv)) return;
+        if (fb && !s->pool.alloc_top(fb, &bf)) {
+            s->pool.release(&bv);
+            return;
+        }
+        if (vb) moves.push_back({r.keep_v.off, bv.off, vb});
+        if (fb) moves.push_back({r.keep_f.off, bf.off, fb});
+        r.move_v = bv;
+        r.move_f = bf;
+    };
+    for (auto &g : sl.groups)
+        for (int64_t id : g.reqs) plan(id);
+    for (int64_t id : sl.singles) plan(id);
+    const uint64_t seq = sl.seq;
+    lk.unlock();
+    cudaError_t e = cudaSuccess;
+    for (const Move &m : moves)
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->arena + m.dst, s->arena + m.src, m.bytes, cudaMemcpyDeviceToDevice, sl.stream);
+    WaveTag *tag = nullptr;
+    if (e == cudaSuccess) {
+        tag = new (std::nothrow) WaveTag{&sl, seq};
+        e = tag ? cudaLaunchHostFunc(sl.stream, moves_done, tag) : cudaErrorMemoryAllocation;
+        if (e != cudaSuccess) delete tag;
+    }
+    lk.lock();
+    if (e != cudaSuccess) {
+        s->msg = std::string("moving finished meshes: ") + cudaGetErrorString(e);
+        fail_wave(s, sl, MESH_ECUDA);
+    }
 }
 
 cudaError_t ensure_pinned(void **p, size_t *cap, size_t n) {
@@ -567,31 +722,6 @@ int launch_wave(mesh_server *s, Slot &sl) {
     return e == cudaSuccess ? MESH_OK : MESH_ECUDA;
 }
 
-// Fails the requests of a wave that will not complete, frees its scratch and
-// the slot.  Called with the lock held.
-void fail_wave(mesh_server *s, Slot &sl, int rc) {
-    for (auto &g : sl.groups) {
-        for (int64_t id : g.reqs) {
-            Req &r = s->reqs[id];
-            r.state = RQ_FAILED;
-            r.status = rc;
-            s->failed++;
-        }
-        s->pool.release(&g.scratch);
-    }
-    for (int64_t id : sl.singles) {
-        Req &r = s->reqs[id];
-        r.state = RQ_FAILED;
-        r.status = rc;
-        s->failed++;
-    }
-    sl.groups.clear();
-    sl.singles.clear();
-    sl.wave.clear();
-    sl.busy = 0;
-    s->cv.notify_all();
-}
-
 void loop(mesh_server *s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
@@ -612,10 +742,19 @@ void loop(mesh_server *s) {
                 }
             }
         };
+        auto finishing = [&]() {
+            for (auto &sl : s->slots)
+                if (sl.busy && sl.finishing) return &sl;
+            return (Slot *)nullptr;
+        };
         while (!s->cv.wait_for(lk, std::chrono::milliseconds(50),
-                               [&] { return s->stop || (!s->queue.empty() && free_slot()); }))
+                               [&] { return s->stop || finishing() || (!s->queue.empty() && free_slot()); }))
             reap();
         if (s->stop) break;
+        if (Slot *fs = finishing()) {
+            finish_wave(s, *fs, lk);
+            continue;
+        }
         Slot &sl = *free_slot();
         form_wave(s, sl);
         if (sl.groups.empty() && sl.singles.empty()) {
@@ -648,8 +787,8 @@ void fill_result(const mesh_server *s, const Req &r, int *state, int64_t *nv, in
     if (state) *state = r.state;
     if (nv) *nv = r.state == RQ_DONE ? r.nverts : 0;
     if (nf) *nf = r.state == RQ_DONE ? r.nfaces : 0;
-    if (v) *v = r.state == RQ_DONE ? (void *)(s->arena + r.out.off) : nullptr;
-    if (f) *f = r.state == RQ_DONE ? (int64_t *)(s->arena + r.out.off + r.vbytes) : nullptr;
+    if (v) *v = r.state == RQ_DONE ? (void *)(s->arena + r.keep_v.off) : nullptr;
+    if (f) *f = r.state == RQ_DONE ? (int64_t *)(s->arena + r.keep_f.off) : nullptr;
 }
 
 }  // namespace
@@ -785,9 +924,9 @@ int mesh_server_release(mesh_server *s, int64_t id) {
     if (it == s->reqs.end()) return sfail(s, MESH_EINVAL, "unknown request");
     if (it->second.state == RQ_QUEUED || it->second.state == RQ_RUNNING)
         return sfail(s, MESH_ESTATE, "request still in flight");
-    s->pool.release(&it->second.out);
-    s->pool.release(&it->second.keep_v);
-    s->pool.release(&it->second.keep_f);
+    for (Block *b : {&it->second.out, &it->second.keep_v, &it->second.keep_f, &it->second.move_v,
+                     &it->second.move_f})
+        s->pool.release(b);
     s->reqs.erase(it);
     s->cv.notify_all();
     return MESH_OK;
