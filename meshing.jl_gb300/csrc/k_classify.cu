@@ -135,6 +135,133 @@ __device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, 
     }
 }
 
+// Marching Cubes table of the walk below: index bits 0..7 are the corners
+// (x,y,z) (x+1,y,z) (x,y,z+1) (x+1,y,z+1) (x,y+1,z) (x+1,y+1,z) (x,y+1,z+1)
+// (x+1,y+1,z+1), i.e. the lane's 2-bit (x, x+1) fields of row y in planes z and
+// z+1, then of row y+1; the word holds the case's vertices (bits 0-11), faces
+// (bits 12-22) and, for an active cell, 1 << 23.
+constexpr uint32_t PK_F = 12, PK_A = 23;
+__device__ __forceinline__ void load_tables_mc_packed(uint32_t *s_tab) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        const unsigned u = (unsigned)i;
+        const unsigned cm = (u & 1u) | (((u >> 1) & 1u) << 1) | (((u >> 5) & 1u) << 2) | (((u >> 4) & 1u) << 3) |
+                            (((u >> 2) & 1u) << 4) | (((u >> 3) & 1u) << 5) | (((u >> 7) & 1u) << 6) |
+                            (((u >> 6) & 1u) << 7);
+        const uint64_t t = MC_CASE_VERTS[cm];
+        s_tab[i] = (uint32_t)((t >> 48) & 15u) | ((uint32_t)((t >> 52) & 7u) << PK_F) |
+                   ((cm != 0u && cm != 255u) ? (1u << PK_A) : 0u);
+    }
+}
+
+// Marching Cubes walk of warp tile (tx, ty) through z segment seg.  Loads and
+// ballots as in classify_tile; a step whose corners are not all on one side
+// costs, per cell row, one lookup in the table above and one add of the
+// packed word (no branch per row or lane).  The words of an activity chunk
+// (ZC planes: at most 12 * ZC vertices, 5 * ZC faces, ZC cells per field) are
+// unpacked at the chunk's end, where a non-zero word marks the row active.
+template <class T>
+__device__ __forceinline__ void classify_tile_mc(const Plan &p, const uint32_t *s_tab, int lane, int tx, int ty,
+                                                 int seg) {
+    static_assert(12 * ZC < (1 << PK_F) && 5 * ZC < (1 << (PK_A - PK_F)) && ZC < (1 << (32 - PK_A)),
+                  "packed chunk counts must not carry into the next field");
+    const int xs = tx * TILE_X + lane;
+    const int y0 = ty * WY;
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    const bool cellx = lane < TILE_X && xs < p.cx;
+    const T *vol = (const T *)p.vol;
+    const int64_t sxy = p.nx * p.ny;
+
+    bool rowok[WY + 1];
+    const T *rowp[WY + 1];
+#pragma unroll
+    for (int r = 0; r <= WY; r++) {
+        rowok[r] = xs < p.nx && y0 + r < p.ny;
+        rowp[r] = rowok[r] ? vol + xs + p.nx * (int64_t)(y0 + r) : vol;
+    }
+    uint32_t rmask[WY];  // the lane's cell of row r exists
+    uint32_t cv[WY], cf[WY], ca[WY];
+#pragma unroll
+    for (int r = 0; r < WY; r++) {
+        rmask[r] = (cellx && y0 + r < p.cy) ? 0xffffffffu : 0u;
+        cv[r] = cf[r] = ca[r] = 0;
+    }
+    const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
+    uint32_t mlo[WY + 1];
+#pragma unroll
+    for (int r = 0; r <= WY; r++) {
+        T v = rowok[r] ? ldv(rowp[r] + sxy * zbeg) : T(0);
+        mlo[r] = __ballot_sync(FULL, rowok[r] && below(v, p));
+    }
+
+    for (int zc0 = zbeg; zc0 < zend; zc0 += ZC) {
+        const int zc1 = min(zc0 + ZC, zend);
+        uint32_t pk[WY];
+#pragma unroll
+        for (int r = 0; r < WY; r++) pk[r] = 0;
+        for (int z = zc0; z < zc1; z += U) {
+            T v[U][WY + 1];
+            const int64_t off = sxy * (int64_t)(z + 1);
+            if (z + U <= zc1) {
+#pragma unroll
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int r = 0; r <= WY; r++) v[u][r] = rowok[r] ? ldv(rowp[r] + off + sxy * u) : T(0);
+            } else {
+#pragma unroll
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int r = 0; r <= WY; r++)
+                        v[u][r] = (rowok[r] && z + 1 + u <= zc1) ? ldv(rowp[r] + off + sxy * u) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (z + u >= zc1) break;  // warp-uniform
+                uint32_t mhi[WY + 1];
+                uint32_t all1 = xval, any1 = 0;
+#pragma unroll
+                for (int r = 0; r <= WY; r++) {
+                    mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
+                    all1 &= mlo[r] & mhi[r];
+                    any1 |= mlo[r] | mhi[r];
+                }
+                // warp-uniform early out: every corner of every cell of this step on one side
+                if (all1 != xval && any1 != 0u) {
+                    uint32_t nb[WY + 1];
+#pragma unroll
+                    for (int r = 0; r <= WY; r++) nb[r] = ((mlo[r] >> lane) & 3u) | (((mhi[r] >> lane) & 3u) << 2);
+#pragma unroll
+                    for (int r = 0; r < WY; r++) pk[r] += s_tab[nb[r] | (nb[r + 1] << 4)] & rmask[r];
+                }
+#pragma unroll
+                for (int r = 0; r <= WY; r++) mlo[r] = mhi[r];
+            }
+        }
+        const int chunk = seg * p.chunks_per_seg + (zc0 - zbeg) / ZC;
+        uint8_t mine = 0;
+#pragma unroll
+        for (int r = 0; r < WY; r++) {
+            const bool act = __any_sync(FULL, pk[r] != 0u);
+            if (lane == r) mine = act;
+            cv[r] += pk[r] & ((1u << PK_F) - 1u);
+            cf[r] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
+            ca[r] += pk[r] >> PK_A;
+        }
+        if (lane < WY && y0 + lane < p.cy) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+    }
+    if (!cellx) return;
+    const int64_t np = p.pstride;
+#pragma unroll
+    for (int r = 0; r < WY; r++) {
+        if (y0 + r < p.cy) {
+            const int64_t i = piece(p, seg, y0 + r, xs);
+            p.cnt[i] = cv[r];
+            p.cnt[np + i] = cf[r];
+            p.cnt[2 * np + i] = ca[r];
+        }
+    }
+}
+
 // Walk of warp tile (tx, ty) through z segment seg with one coalesced global
 // load per lane, row and plane (any layout).
 template <class T, int ALG>
@@ -201,11 +328,17 @@ __device__ __forceinline__ void classify_tile(const Plan &p, const uint32_t *s_t
 template <class T, int ALG>
 __global__ void __launch_bounds__(256) k_classify(const Plan p) {
     __shared__ uint32_t s_tab[256];
-    load_tables<ALG>(s_tab);
+    if (ALG == MESH_ALG_MC)
+        load_tables_mc_packed(s_tab);
+    else
+        load_tables<ALG>(s_tab);
     __syncthreads();
     const int ty = blockIdx.y * WARPS + (threadIdx.x >> 5);
     if (ty * CWY >= p.cy) return;  // warp-uniform
-    classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
+    if (ALG == MESH_ALG_MC)
+        classify_tile_mc<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
+    else
+        classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
 }
 
 // Batch (Marching Cubes): persistent warps take work items -- a warp tile of
@@ -213,7 +346,7 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
 template <class T>
 __global__ void __launch_bounds__(256) k_classify_batch(const Plan p) {
     __shared__ uint32_t s_tab[256];
-    load_tables<MESH_ALG_MC>(s_tab);
+    load_tables_mc_packed(s_tab);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -227,7 +360,7 @@ __global__ void __launch_bounds__(256) k_classify_batch(const Plan p) {
         const int ty = (int)(local % b.tiles_y);
         const int tx = (int)((local / b.tiles_y) % b.tiles_x);
         const int seg = (int)(local / ((int64_t)b.tiles_y * b.tiles_x));
-        classify_tile<T, MESH_ALG_MC>(pv, s_tab, lane, tx, ty, seg);
+        classify_tile_mc<T>(pv, s_tab, lane, tx, ty, seg);
     }
 }
 
