@@ -14,6 +14,7 @@
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
+#include "mesh_case.cuh"
 #include "mesh_tma.cuh"
 
 #include <algorithm>
@@ -135,35 +136,15 @@ __device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, 
     }
 }
 
-// Marching Cubes table of the walk below: index bits 0..7 are the corners
-// (x,y,z) (x+1,y,z) (x,y,z+1) (x+1,y,z+1) (x,y+1,z) (x+1,y+1,z) (x,y+1,z+1)
-// (x+1,y+1,z+1), i.e. the lane's 2-bit (x, x+1) fields of row y in planes z and
-// z+1, then of row y+1; the word holds the case's vertices (bits 0-11), faces
-// (bits 12-22) and, for an active cell, 1 << 23.
-constexpr uint32_t PK_F = 12, PK_A = 23;
-__device__ __forceinline__ void load_tables_mc_packed(uint32_t *s_tab) {
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-        const unsigned u = (unsigned)i;
-        const unsigned cm = (u & 1u) | (((u >> 1) & 1u) << 1) | (((u >> 5) & 1u) << 2) | (((u >> 4) & 1u) << 3) |
-                            (((u >> 2) & 1u) << 4) | (((u >> 3) & 1u) << 5) | (((u >> 7) & 1u) << 6) |
-                            (((u >> 6) & 1u) << 7);
-        const uint64_t t = MC_CASE_VERTS[cm];
-        s_tab[i] = (uint32_t)((t >> 48) & 15u) | ((uint32_t)((t >> 52) & 7u) << PK_F) |
-                   ((cm != 0u && cm != 255u) ? (1u << PK_A) : 0u);
-    }
-}
-
 // Marching Cubes walk of warp tile (tx, ty) through z segment seg.  Loads and
 // ballots as in classify_tile; a step whose corners are not all on one side
-// costs, per cell row, one lookup in the table above and one add of the
-// packed word (no branch per row or lane).  The words of an activity chunk
+// costs, per cell row, one lookup of the case's packed word (mesh_case.cuh)
+// and one add (no branch per row or lane).  The words of an activity chunk
 // (ZC planes: at most 12 * ZC vertices, 5 * ZC faces, ZC cells per field) are
 // unpacked at the chunk's end, where a non-zero word marks the row active.
 template <class T>
 __device__ __forceinline__ void classify_tile_mc(const Plan &p, const uint32_t *s_tab, int lane, int tx, int ty,
                                                  int seg) {
-    static_assert(12 * ZC < (1 << PK_F) && 5 * ZC < (1 << (PK_A - PK_F)) && ZC < (1 << (32 - PK_A)),
-                  "packed chunk counts must not carry into the next field");
     const int xs = tx * TILE_X + lane;
     const int y0 = ty * WY;
     const int zbeg = seg * p.zs;
@@ -229,7 +210,7 @@ __device__ __forceinline__ void classify_tile_mc(const Plan &p, const uint32_t *
                 if (all1 != xval && any1 != 0u) {
                     uint32_t nb[WY + 1];
 #pragma unroll
-                    for (int r = 0; r <= WY; r++) nb[r] = ((mlo[r] >> lane) & 3u) | (((mhi[r] >> lane) & 3u) << 2);
+                    for (int r = 0; r <= WY; r++) nb[r] = row_field(mlo[r], mhi[r], lane);
 #pragma unroll
                     for (int r = 0; r < WY; r++) pk[r] += s_tab[nb[r] | (nb[r + 1] << 4)] & rmask[r];
                 }

@@ -19,6 +19,7 @@
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
+#include "mesh_case.cuh"
 #include "mesh_mc.cuh"
 
 #include <algorithm>
@@ -34,62 +35,94 @@ static_assert(ZC % U == 0, "U must divide the activity chunk");
 
 // ---------------------------------------------------------------- K3a ----
 
+// Shared memory of a compaction CTA: the case tables and, per warp, the
+// global vertex / face offsets of the lanes' pieces (needed only at chunk ends
+// and for the side words, so they stay out of registers).
+struct CompactSmem {
+    uint32_t pk[256];
+    uint8_t cs[256];
+    long long bv[WARPS][WY][32], bf[WARPS][WY][32];
+};
+
 // Entries of warp tile (tx, ty) of z segment seg; with a batch, each entry
-// also records its volume `vol`.
+// also records its volume `vol`.  The activity bytes of 32 chunks are read at
+// once and the walk visits only the active chunks.  Inside a chunk a step whose corners are not all on one side costs,
+// per cell row, one lookup of the case's packed word (mesh_case.cuh); the
+// lanes whose cell is active write its entry at the piece's entry offset plus
+// the entries before it in the chunk (bits 23.. of the running word).
 template <class T>
-__device__ __forceinline__ void compact_tile(const Plan &p, const uint64_t *s_v, int lane, int tx, int ty, int seg,
+__device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int w, int lane, int tx, int ty, int seg,
                                              uint32_t vol) {
     const T *volp = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
     const int64_t np = p.pstride;
-    {
-        const int xs = tx * TILE_X + lane;
-        const int y0 = ty * WY;
-        const int zbeg = seg * p.zs;
-        const int zend = min(zbeg + p.zs, p.cz);
-        const bool cellx = lane < TILE_X && xs < p.cx;
+    const int xs = tx * TILE_X + lane;
+    const int y0 = ty * WY;
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    const bool cellx = lane < TILE_X && xs < p.cx;
 
-        bool rowok[WY + 1];
-        const T *rowp[WY + 1];
+    bool rowok[WY + 1];
+    const T *rowp[WY + 1];
 #pragma unroll
-        for (int r = 0; r <= WY; r++) {
-            rowok[r] = xs < p.nx && y0 + r < p.ny;
-            rowp[r] = rowok[r] ? volp + xs + p.nx * (int64_t)(y0 + r) : volp;
-        }
-        const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
-        const uint32_t cellm = __ballot_sync(FULL, cellx);
-        int64_t bv[WY], bf[WY], ba[WY];  // running vertex / face / entry offsets of each row's cell
+    for (int r = 0; r <= WY; r++) {
+        rowok[r] = xs < p.nx && y0 + r < p.ny;
+        rowp[r] = rowok[r] ? volp + xs + p.nx * (int64_t)(y0 + r) : volp;
+    }
+    const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
+    uint32_t rmask[WY];
+    int64_t ba[WY];  // entry offset of each row's piece
 #pragma unroll
-        for (int r = 0; r < WY; r++) {
-            bv[r] = bf[r] = ba[r] = 0;
-            if (cellx && y0 + r < p.cy) {
-                const int64_t i = piece(p, seg, y0 + r, xs);
-                bv[r] = p.base[i];
-                bf[r] = p.base[np + i];
-                ba[r] = p.base[2 * np + i];
-            }
+    for (int r = 0; r < WY; r++) {
+        rmask[r] = (cellx && y0 + r < p.cy) ? 0xffffffffu : 0u;
+        ba[r] = 0;
+        long long v0 = 0, f0 = 0;
+        if (rmask[r]) {
+            const int64_t i = piece(p, seg, y0 + r, xs);
+            v0 = p.base[i];
+            f0 = p.base[np + i];
+            ba[r] = p.base[2 * np + i];
         }
+        sm.bv[w][r][lane] = v0;
+        sm.bf[w][r][lane] = f0;
+    }
+    __syncwarp();
 
-        uint32_t mlo[WY + 1];
-        T lov[WY + 1];  // samples of plane z
-        bool have_lo = false;
-        for (int zc0 = zbeg; zc0 < zend; zc0 += ZC) {
+    // activity of chunks [32 g, 32 g + 32): lane l reads chunk 32 g + l's row bytes
+    const int nch = (zend - zbeg + ZC - 1) / ZC;
+    const int64_t chunk0 = (int64_t)seg * p.chunks_per_seg;
+    auto active = [&](int g) {
+        const int k = 32 * g + lane;
+        uint32_t any = 0;
+        if (k < nch) {
+            const uint8_t *fp = p.flags + ((chunk0 + k) * p.tiles_x + tx) * p.cy + y0;
+#pragma unroll
+            for (int r = 0; r < WY; r++)
+                if (y0 + r < p.cy) any |= fp[r];
+        }
+        return __ballot_sync(FULL, any != 0u);
+    };
+
+    uint32_t mlo[WY + 1];
+    T lov[WY + 1];  // samples of plane `have`
+    int have = -1;
+    for (int g = 0; 32 * g < nch; g++) {
+        uint32_t todo = active(g);
+        while (todo) {
+            const int k = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int zc0 = zbeg + k * ZC + 32 * g * ZC;
             const int zc1 = min(zc0 + ZC, zend);
-            const int chunk = seg * p.chunks_per_seg + (zc0 - zbeg) / ZC;
-            uint8_t f = 0;
-            if (lane < WY && y0 + lane < p.cy) f = p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane];
-            if (!__any_sync(FULL, f != 0)) {
-                have_lo = false;
-                continue;
-            }
-            if (!have_lo) {
+            if (have != zc0) {
 #pragma unroll
                 for (int r = 0; r <= WY; r++) {
                     lov[r] = rowok[r] ? ldv(rowp[r] + sxy * (int64_t)zc0) : T(0);
                     mlo[r] = __ballot_sync(FULL, rowok[r] && below(lov[r], p));
                 }
-                have_lo = true;
             }
+            uint32_t pk[WY];
+#pragma unroll
+            for (int r = 0; r < WY; r++) pk[r] = 0;
             for (int z = zc0; z < zc1; z += U) {
                 T v[U][WY + 1];
                 const int64_t off = sxy * (int64_t)(z + 1);
@@ -101,7 +134,7 @@ __device__ __forceinline__ void compact_tile(const Plan &p, const uint64_t *s_v,
 #pragma unroll
                 for (int u = 0; u < U; u++) {
                     const int zc = z + u;
-                    if (zc >= zc1) break;
+                    if (zc >= zc1) break;  // warp-uniform
                     uint32_t mhi[WY + 1];
                     uint32_t all1 = xval, any1 = 0;
 #pragma unroll
@@ -110,45 +143,47 @@ __device__ __forceinline__ void compact_tile(const Plan &p, const uint64_t *s_v,
                         all1 &= mlo[r] & mhi[r];
                         any1 |= mlo[r] | mhi[r];
                     }
-                    if (all1 != xval && any1 != 0) {
+                    if (all1 != xval && any1 != 0u) {
+                        // corner values of row r in plane z (l0) and z+1 (h0), x+1 from
+                        // the next lane (l1, h1); row r+1 likewise (L0 L1 H0 H1)
+                        T l0 = u == 0 ? lov[0] : v[u == 0 ? 0 : u - 1][0];
+                        T h0 = v[u][0];
+                        T l1 = shfl_down1(l0), h1 = shfl_down1(h0);
+                        uint32_t n0 = row_field(mlo[0], mhi[0], lane);
 #pragma unroll
                         for (int r = 0; r < WY; r++) {
-                            const uint32_t and4 = mlo[r] & mlo[r + 1] & mhi[r] & mhi[r + 1];
-                            const uint32_t or4 = mlo[r] | mlo[r + 1] | mhi[r] | mhi[r + 1];
-                            const uint32_t actm = (or4 | (or4 >> 1)) & ~(and4 & (and4 >> 1)) & cellm;
-                            if (actm == 0u || y0 + r >= p.cy) continue;  // warp-uniform
-                            // corner values; x+1 from the next lane
-                            const T a0 = u == 0 ? lov[r] : v[u == 0 ? 0 : u - 1][r];
-                            const T b0 = u == 0 ? lov[r + 1] : v[u == 0 ? 0 : u - 1][r + 1];
-                            const T c0 = v[u][r], d0 = v[u][r + 1];
-                            const T a1 = shfl_down1(a0), b1 = shfl_down1(b0), c1 = shfl_down1(c0), d1 = shfl_down1(d0);
-                            if ((actm >> lane) & 1u) {
-                                const unsigned a = (mlo[r] >> lane) & 3u, b = (mlo[r + 1] >> lane) & 3u;
-                                const unsigned c = (mhi[r] >> lane) & 3u, d = (mhi[r + 1] >> lane) & 3u;
-                                const unsigned cm = (a & 1u) | ((a >> 1) << 1) | ((b >> 1) << 2) | ((b & 1u) << 3) |
-                                                    ((c & 1u) << 4) | ((c >> 1) << 5) | ((d >> 1) << 6) |
-                                                    ((d & 1u) << 7);
-                                const int64_t e = ba[r];
+                            const T L0 = u == 0 ? lov[r + 1] : v[u == 0 ? 0 : u - 1][r + 1];
+                            const T H0 = v[u][r + 1];
+                            const T L1 = shfl_down1(L0), H1 = shfl_down1(H0);
+                            const uint32_t n1 = row_field(mlo[r + 1], mhi[r + 1], lane);
+                            const unsigned idx = n0 | (n1 << 4);
+                            const uint32_t t = sm.pk[idx] & rmask[r];
+                            if (t) {
+                                const int64_t e = ba[r] + (pk[r] >> PK_A);
                                 if (e < p.ent_cap) {
                                     p.ent_pos[e] = (unsigned long long)xs |
                                                    ((unsigned long long)(y0 + r) << POS_BITS) |
                                                    ((unsigned long long)zc << (2 * POS_BITS));
-                                    p.ent_cs[e] = (uint8_t)cm;
-                                    const T cv[8] = {a0, a1, b1, b0, c0, c1, d1, d0};
+                                    p.ent_cs[e] = sm.cs[idx];
+                                    const T cv[8] = {l0, l1, L1, L0, h0, h1, H1, H0};
                                     store8<T>((T *)p.ent_val + 8 * e, cv);
                                     if (p.ent_vol) p.ent_vol[e] = vol;
                                     if ((e & (ENT_BLOCK - 1)) == 0) {
-                                        p.ent_side[2 * (e / ENT_BLOCK)] = bv[r];
-                                        p.ent_side[2 * (e / ENT_BLOCK) + 1] = bf[r];
+                                        p.ent_side[2 * (e / ENT_BLOCK)] =
+                                            sm.bv[w][r][lane] + (pk[r] & ((1u << PK_F) - 1u));
+                                        p.ent_side[2 * (e / ENT_BLOCK) + 1] =
+                                            sm.bf[w][r][lane] + ((pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u));
                                     }
                                 } else {
                                     atomicOr(p.err, ERR_CAPACITY);
                                 }
-                                const uint64_t t = s_v[cm];
-                                ba[r] = e + 1;
-                                bv[r] += (int64_t)((t >> 48) & 15u);
-                                bf[r] += (int64_t)((t >> 52) & 7u);
+                                pk[r] += t;
                             }
+                            l0 = L0;
+                            l1 = L1;
+                            h0 = H0;
+                            h1 = H1;
+                            n0 = n1;
                         }
                     }
 #pragma unroll
@@ -157,16 +192,26 @@ __device__ __forceinline__ void compact_tile(const Plan &p, const uint64_t *s_v,
 #pragma unroll
                 for (int r = 0; r <= WY; r++) lov[r] = v[U - 1][r];
             }
+            // a chunk of ZC planes ends on whole groups of U (ZC % U == 0), so
+            // lov / mlo hold plane zc1; after a shorter last chunk nothing follows
+            have = zc1;
+#pragma unroll
+            for (int r = 0; r < WY; r++) {
+                ba[r] += pk[r] >> PK_A;
+                sm.bv[w][r][lane] += pk[r] & ((1u << PK_F) - 1u);
+                sm.bf[w][r][lane] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
+            }
         }
     }
+    __syncwarp();
 }
 
 template <class T>
 __global__ void __launch_bounds__(256, 2) k_compact_mc(const Plan p, int nitems) {
-    __shared__ uint64_t s_v[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
+    __shared__ CompactSmem sm;
+    load_tables_mc_packed(sm.pk, sm.cs);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     // persistent warps: take (y tile, x tile, segment) items in order from a counter
     for (;;) {
         int item = 0;
@@ -176,17 +221,17 @@ __global__ void __launch_bounds__(256, 2) k_compact_mc(const Plan p, int nitems)
         const int ty = item % p.tiles_y;
         const int tx = (item / p.tiles_y) % p.tiles_x;
         const int seg = item / (p.tiles_y * p.tiles_x);
-        compact_tile<T>(p, s_v, lane, tx, ty, seg, 0);
+        compact_tile<T>(p, sm, w, lane, tx, ty, seg, 0);
     }
 }
 
 // Batch: the work items of k_classify_batch, in the same order.
 template <class T>
 __global__ void __launch_bounds__(256, 2) k_compact_batch(const Plan p) {
-    __shared__ uint64_t s_v[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_v[i] = MC_CASE_VERTS[i];
+    __shared__ CompactSmem sm;
+    load_tables_mc_packed(sm.pk, sm.cs);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (;;) {
         unsigned item = 0;
         if (lane == 0) item = atomicAdd(p.work, 1u);
@@ -198,7 +243,7 @@ __global__ void __launch_bounds__(256, 2) k_compact_batch(const Plan p) {
         const int ty = (int)(local % b.tiles_y);
         const int tx = (int)((local / b.tiles_y) % b.tiles_x);
         const int seg = (int)(local / ((int64_t)b.tiles_y * b.tiles_x));
-        compact_tile<T>(vol_view(p, b), s_v, lane, tx, ty, seg, v);
+        compact_tile<T>(vol_view(p, b), sm, w, lane, tx, ty, seg, v);
     }
 }
 
