@@ -136,6 +136,98 @@ __device__ __forceinline__ void store_counts(const Plan &p, bool cellx, int xs, 
     }
 }
 
+// The walk below for a warp tile inside the volume (all 32 lanes' samples and
+// all WY + 1 rows exist) whose z segment spans fewer than 2^32 samples: no
+// per-lane or per-row guards, 32-bit sample offsets from the segment's first
+// plane, and each plane's row masks reduced once (AND / OR over the rows) for
+// the one-side test of the two steps that use it.  Counts equal the walk
+// below; lane 31 (no cell) is left out of the activity bytes and the counts.
+template <class T>
+__device__ __forceinline__ void classify_tile_mc_inner(const Plan &p, const uint32_t *s_tab, int lane, int tx,
+                                                       int ty, int seg) {
+    const int xs = tx * TILE_X + lane;
+    const int y0 = ty * WY;
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    const uint32_t sxy = (uint32_t)(p.nx * p.ny), nx = (uint32_t)p.nx;
+    const T *base = (const T *)p.vol + (int64_t)sxy * zbeg + xs + p.nx * (int64_t)y0;
+    constexpr uint32_t CELLM = 0x7fffffffu;  // lanes 0..30 own cells
+
+    uint32_t cv[WY], cf[WY], ca[WY];
+#pragma unroll
+    for (int r = 0; r < WY; r++) cv[r] = cf[r] = ca[r] = 0;
+    uint32_t mlo[WY + 1];
+#pragma unroll
+    for (int r = 0; r <= WY; r++) mlo[r] = __ballot_sync(FULL, below(ldv(base + r * nx), p));
+    uint32_t alo = mlo[0] & mlo[1] & mlo[2] & mlo[3] & mlo[4], olo = mlo[0] | mlo[1] | mlo[2] | mlo[3] | mlo[4];
+    static_assert(WY == 4, "the plane reductions below name rows 0..4");
+    uint32_t zoff = 0;  // plane zc0 relative to zbeg
+
+    for (int zc0 = zbeg; zc0 < zend; zc0 += ZC) {
+        const int n = min(ZC, zend - zc0);
+        uint32_t pk[WY];
+#pragma unroll
+        for (int r = 0; r < WY; r++) pk[r] = 0;
+        for (int u0 = 0; u0 < n; u0 += U) {
+            T v[U][WY + 1];
+            if (u0 + U <= n) {
+#pragma unroll
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int r = 0; r <= WY; r++) v[u][r] = ldv(base + (zoff + (u + 1) * sxy + r * nx));
+            } else {
+#pragma unroll
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int r = 0; r <= WY; r++)
+                        v[u][r] = u0 + u < n ? ldv(base + (zoff + (u + 1) * sxy + r * nx)) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (u0 + u >= n) break;  // warp-uniform
+                uint32_t mhi[WY + 1];
+#pragma unroll
+                for (int r = 0; r <= WY; r++) mhi[r] = __ballot_sync(FULL, below(v[u][r], p));
+                const uint32_t ahi = mhi[0] & mhi[1] & mhi[2] & mhi[3] & mhi[4];
+                const uint32_t ohi = mhi[0] | mhi[1] | mhi[2] | mhi[3] | mhi[4];
+                if ((alo & ahi) != FULL && (olo | ohi) != 0u) {
+                    uint32_t nb[WY + 1];
+#pragma unroll
+                    for (int r = 0; r <= WY; r++) nb[r] = row_field(mlo[r], mhi[r], lane);
+#pragma unroll
+                    for (int r = 0; r < WY; r++) pk[r] += s_tab[nb[r] | (nb[r + 1] << 4)];
+                }
+#pragma unroll
+                for (int r = 0; r <= WY; r++) mlo[r] = mhi[r];
+                alo = ahi;
+                olo = ohi;
+            }
+            zoff += U * sxy;
+        }
+        zoff += (uint32_t)(n - (n + U - 1) / U * U) * sxy;  // back to plane zc0 + n after a short chunk
+        const int chunk = seg * p.chunks_per_seg + (zc0 - zbeg) / ZC;
+        uint8_t mine = 0;
+#pragma unroll
+        for (int r = 0; r < WY; r++) {
+            const bool act = (__ballot_sync(FULL, pk[r] != 0u) & CELLM) != 0u;
+            if (lane == r) mine = act;
+            cv[r] += pk[r] & ((1u << PK_F) - 1u);
+            cf[r] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
+            ca[r] += pk[r] >> PK_A;
+        }
+        if (lane < WY) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+    }
+    if (lane >= TILE_X) return;
+    const int64_t np = p.pstride;
+#pragma unroll
+    for (int r = 0; r < WY; r++) {
+        const int64_t i = piece(p, seg, y0 + r, xs);
+        p.cnt[i] = cv[r];
+        p.cnt[np + i] = cf[r];
+        p.cnt[2 * np + i] = ca[r];
+    }
+}
+
 // Marching Cubes walk of warp tile (tx, ty) through z segment seg.  Loads and
 // ballots as in classify_tile; a step whose corners are not all on one side
 // costs, per cell row, one lookup of the case's packed word (mesh_case.cuh)
@@ -316,9 +408,12 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
     __syncthreads();
     const int ty = blockIdx.y * WARPS + (threadIdx.x >> 5);
     if (ty * CWY >= p.cy) return;  // warp-uniform
-    if (ALG == MESH_ALG_MC)
-        classify_tile_mc<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
-    else
+    if (ALG == MESH_ALG_MC) {
+        if (tile_inner(p, blockIdx.x, ty, blockIdx.z))
+            classify_tile_mc_inner<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
+        else
+            classify_tile_mc<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
+    } else
         classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
 }
 

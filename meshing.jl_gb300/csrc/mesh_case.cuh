@@ -40,5 +40,15 @@ __device__ __forceinline__ uint32_t row_field(uint32_t mlo, uint32_t mhi, int la
     return ((mlo >> lane) & 3u) | (((mhi >> lane) & 3u) << 2);
 }
 
+// Whether warp tile (tx, ty) of z segment seg lies inside the volume (all 32
+// lanes' samples and all WY + 1 sample rows exist) with a segment of fewer
+// than 2^32 samples: the walks then take their guard-free form.
+__device__ __forceinline__ bool tile_inner(const Plan &p, int tx, int ty, int seg) {
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    return (int64_t)tx * TILE_X + 32 <= p.nx && (int64_t)ty * WY + WY <= p.cy &&
+           (int64_t)(zend - zbeg + 1) * p.nx * p.ny <= (int64_t)0xffffffffu;
+}
+
 }  // namespace
 }  // namespace mesh
