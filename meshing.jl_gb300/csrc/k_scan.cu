@@ -8,15 +8,24 @@
 // the counts sit in memory as [seg][y][x] (x fastest, written coalesced by
 // the classify kernel).
 //
-// One CTA scans 32 columns (lane = x, so every access stays coalesced): its
-// 32 warps split the (y, seg) sequence of every column, reduce, scan across
-// warps through shared memory (one warp per counter: vertices, faces, active
-// cells), scan the 32 column totals with warp shuffles,
-// and chain the groups of 32 columns with a single-pass decoupled look-back
-// (groups are taken in ticket order, so every predecessor is already
-// resident).  Look-back waits are bounded: on expiry the kernel sets
-// ERR_SCAN_TIMEOUT in the device error word and finishes without hanging.
+// Single volume (k_scan_reduce, k_scan_cols, k_scan_colsum, k_scan_down): the
+// (y, seg) sequence of every column is cut into C runs; a warp takes one run of
+// 32 columns (lane = x, so every access stays coalesced) and sums it; a warp
+// per column scans its run sums, three CTAs scan the column sums (x order),
+// and the warps walk their runs again writing the offsets.  No wait between
+// CTAs.
+//
+// Batch (k_scan_batch): one CTA scans 32 columns of one volume: its warps
+// split the (y, seg) sequence of every column, reduce, scan across warps
+// through shared memory (one warp per counter: vertices, faces, active cells),
+// scan the 32 column totals with warp shuffles, and chain the groups of 32
+// columns of all volumes with a single-pass decoupled look-back (groups are
+// taken in ticket order, so every predecessor is already resident).
+// Look-back waits are bounded: on expiry the kernel sets ERR_SCAN_TIMEOUT in
+// the device error word and finishes without hanging.
 #include "mesh_internal.cuh"
+
+#include <algorithm>
 
 namespace mesh {
 
@@ -184,13 +193,198 @@ __device__ __forceinline__ void scan_body(const Plan &p, int xt, int gt, int nti
     }
 }
 
-__global__ void __launch_bounds__(1024) k_scan(const Plan p, int ntiles) {
-    __shared__ int s_tile;
-    __shared__ int64_t s_part[NCNT][32][33];
-    __shared__ int64_t s_xpre[NCNT][32];
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.scan_ticket, 1u);
+// ---- single volume: reduce, scan of the run sums, downsweep ----
+
+// Runs per column and steps per run for a plan: at most 128 runs (the column
+// scan takes 4 rounds of 32) of at least 16 steps, and at most 2^20 run sums
+// per counter.
+struct ScanGeom {
+    int G, C;     // column groups of 32, runs per column
+    int64_t per;  // (y, seg) steps per run
+};
+inline ScanGeom scan_geom(const Plan &p) {
+    ScanGeom g;
+    g.G = (p.cx + 31) / 32;
+    const int64_t L = (int64_t)p.cy * p.nseg;
+    int64_t C = std::min<int64_t>(128, std::max<int64_t>(1, L / 16));
+    C = std::min<int64_t>(C, std::max<int64_t>(1, ((int64_t)1 << 20) / (32 * (int64_t)g.G)));
+    g.C = (int)std::max<int64_t>(1, C);
+    g.per = (L + g.C - 1) / g.C;
+    return g;
+}
+
+// Piece index of step j of column x: (seg, y) with seg fastest.
+struct ColWalk {
+    int64_t i;
+    int seg;
+    __device__ ColWalk(const Plan &p, int64_t j, int x) {
+        seg = (int)(j % p.nseg);
+        i = piece(p, seg, (int)(j / p.nseg), x);
+    }
+    __device__ void next(const Plan &p) {
+        if (++seg == p.nseg) {
+            seg = 0;
+            i += (int64_t)p.cx - (int64_t)(p.nseg - 1) * p.cy * p.cx;
+        } else {
+            i += (int64_t)p.cy * p.cx;
+        }
+    }
+};
+
+// part[k][x][c]: sum of counter k over run c of column x (x < 32 G; columns past
+// cx sum to 0).
+__global__ void __launch_bounds__(256) k_scan_reduce(const Plan p, int G, int C, int64_t per) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int c = blockIdx.y * 8 + w;
+    if (c >= C) return;  // warp-uniform
+    const int x = blockIdx.x * 32 + lane;
+    const int64_t L = (int64_t)p.cy * p.nseg;
+    const int64_t j0 = min(L, (int64_t)c * per), j1 = min(L, j0 + per);
+    const int64_t np = p.pstride;
+    int64_t sum[NCNT] = {0, 0, 0};
+    static_assert(NCNT == 3, "three counters");
+    if (x < p.cx) {
+        ColWalk cw(p, j0, x);
+        int64_t j = j0;
+        constexpr int UN = 4;
+        for (; j + UN <= j1; j += UN) {
+            int64_t ii[UN];
+#pragma unroll
+            for (int k = 0; k < UN; k++) {
+                ii[k] = cw.i;
+                cw.next(p);
+            }
+#pragma unroll
+            for (int k = 0; k < NCNT; k++)
+#pragma unroll
+                for (int u = 0; u < UN; u++) sum[k] += p.cnt[k * np + ii[u]];
+        }
+        for (; j < j1; j++) {
+#pragma unroll
+            for (int k = 0; k < NCNT; k++) sum[k] += p.cnt[k * np + cw.i];
+            cw.next(p);
+        }
+    }
+    long long *part = (long long *)p.scan_state;
+    const int64_t E = (int64_t)32 * G * C;
+#pragma unroll
+    for (int k = 0; k < NCNT; k++) part[k * E + (int64_t)x * C + c] = sum[k];
+}
+
+// Per column (a warp per counter and column): the run sums become exclusive
+// prefixes inside the column, and the column's total goes to col[k][x].
+__global__ void __launch_bounds__(256) k_scan_cols(const Plan p, int G, int C) {
+    const int lane = threadIdx.x & 31;
+    const int64_t ncol = (int64_t)32 * G;
+    const int64_t wid = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (wid >= NCNT * ncol) return;  // warp-uniform
+    const int k = (int)(wid / ncol);
+    const int64_t x = wid % ncol;
+    long long *r = (long long *)p.scan_state + (k * ncol + x) * C;
+    long long *col = (long long *)p.scan_state + (int64_t)NCNT * ncol * C;
+    long long carry = 0;
+    for (int c0 = 0; c0 < C; c0 += 32) {  // C <= 128: at most 4 rounds
+        const int c = c0 + lane;
+        const long long v = c < C ? r[c] : 0;
+        long long inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long u = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (c < C) r[c] = carry + inc - v;
+        carry += __shfl_sync(FULL, inc, 31);
+    }
+    if (lane == 0) col[k * ncol + x] = carry;
+}
+
+// In place: col[k][x] becomes the exclusive prefix of column x; totals[k] the
+// sum of all.  CTA k scans counter k; a thread owns a contiguous range of columns.
+__global__ void __launch_bounds__(1024) k_scan_colsum(const Plan p, int G, int C) {
+    __shared__ long long s_w[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int k = blockIdx.x;
+    const int64_t ncol = (int64_t)32 * G;
+    long long *a = (long long *)p.scan_state + (int64_t)NCNT * ncol * C + k * ncol;
+    const int64_t q = (ncol + 1023) / 1024;
+    const int64_t x0 = min(ncol, (int64_t)tid * q), x1 = min(ncol, x0 + q);
+    long long sum = 0;
+    for (int64_t x = x0; x < x1; x++) sum += a[x];
+    long long inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) s_w[w] = inc;
     __syncthreads();
-    scan_body(p, s_tile, s_tile, ntiles, s_part, s_xpre);
+    if (w == 0) {
+        const long long v = s_w[lane];
+        long long vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long u = __shfl_up_sync(FULL, vi, o);
+            if (lane >= o) vi += u;
+        }
+        s_w[lane] = vi - v;  // exclusive prefix of warp `lane`
+        if (lane == 31) p.totals[k] = vi;
+    }
+    __syncthreads();
+    long long run = s_w[w] + inc - sum;
+    for (int64_t x = x0; x < x1; x++) {
+        const long long v = a[x];
+        a[x] = run;
+        run += v;
+    }
+}
+
+// Each warp walks its run again, writing base[k] of every piece.
+__global__ void __launch_bounds__(256) k_scan_down(const Plan p, int G, int C, int64_t per) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int c = blockIdx.y * 8 + w;
+    if (c >= C) return;  // warp-uniform
+    const int x = blockIdx.x * 32 + lane;
+    if (x >= p.cx) return;
+    const int64_t L = (int64_t)p.cy * p.nseg;
+    const int64_t j0 = min(L, (int64_t)c * per), j1 = min(L, j0 + per);
+    const int64_t np = p.pstride;
+    const long long *part = (const long long *)p.scan_state;
+    const int64_t ncol = (int64_t)32 * G, E = ncol * C;
+    const long long *col = part + NCNT * E;
+    int64_t b[NCNT];
+#pragma unroll
+    for (int k = 0; k < NCNT; k++) b[k] = col[k * ncol + x] + part[k * E + (int64_t)x * C + c];
+    ColWalk cw(p, j0, x);
+    int64_t j = j0;
+    constexpr int UN = 4;
+    for (; j + UN <= j1; j += UN) {
+        int64_t ii[UN];
+        uint32_t v[NCNT][UN];
+#pragma unroll
+        for (int u = 0; u < UN; u++) {
+            ii[u] = cw.i;
+            cw.next(p);
+        }
+#pragma unroll
+        for (int k = 0; k < NCNT; k++)
+#pragma unroll
+            for (int u = 0; u < UN; u++) v[k][u] = p.cnt[k * np + ii[u]];
+#pragma unroll
+        for (int u = 0; u < UN; u++)
+#pragma unroll
+            for (int k = 0; k < NCNT; k++) {
+                p.base[k * np + ii[u]] = b[k];
+                b[k] += v[k][u];
+            }
+    }
+    for (; j < j1; j++) {
+#pragma unroll
+        for (int k = 0; k < NCNT; k++) {
+            p.base[k * np + cw.i] = b[k];
+            b[k] += p.cnt[k * np + cw.i];
+        }
+        cw.next(p);
+    }
 }
 
 // Batch: the scan tiles of all volumes, volumes in order, form one look-back
@@ -227,7 +421,11 @@ __global__ void k_batch_offsets(const Plan p) {
 
 }  // namespace
 
-int scan_tiles(const Plan &p) { return (p.cx + 31) / 32; }
+// Bytes of the scan scratch (scan_state) of a single-volume plan.
+size_t scan_scratch_bytes(const Plan &p) {
+    const ScanGeom g = scan_geom(p);
+    return (size_t)NCNT * 32 * g.G * (g.C + 1) * sizeof(long long);  // run sums, column sums
+}
 
 cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * NCNT * (size_t)p.nstiles, s);
@@ -242,12 +440,12 @@ cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s) {
 }
 
 cudaError_t launch_scan(const Plan &p, cudaStream_t s) {
-    const int ntiles = scan_tiles(p);
-    cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * NCNT * (size_t)ntiles, s);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(p.scan_ticket, 0, sizeof(unsigned int), s);
-    if (e != cudaSuccess) return e;
-    k_scan<<<ntiles, 1024, 0, s>>>(p, ntiles);
+    const ScanGeom g = scan_geom(p);
+    const dim3 grid(g.G, (g.C + 7) / 8);
+    k_scan_reduce<<<grid, 256, 0, s>>>(p, g.G, g.C, g.per);
+    k_scan_cols<<<(int)((NCNT * 32 * (int64_t)g.G + 7) / 8), 256, 0, s>>>(p, g.G, g.C);
+    k_scan_colsum<<<NCNT, 1024, 0, s>>>(p, g.G, g.C);
+    k_scan_down<<<grid, 256, 0, s>>>(p, g.G, g.C, g.per);
     return cudaGetLastError();
 }
 

@@ -29,7 +29,7 @@ namespace mesh {
 cudaError_t launch_classify_tma(const Plan &p, const CUtensorMap &map, cudaStream_t s);
 cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStream_t s);
 cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
-int scan_tiles(const Plan &p);
+size_t scan_scratch_bytes(const Plan &p);
 }  // namespace mesh
 
 using namespace mesh;
@@ -237,14 +237,13 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     if ((e = c->base.ensure((size_t)np * NCNT * sizeof(int64_t))) != cudaSuccess) return cuda_fail(c, e, "base buffer");
     const size_t fb = (size_t)P.nchunks * P.tiles_x * P.cy;
     if ((e = c->flags.ensure(fb)) != cudaSuccess) return cuda_fail(c, e, "flag buffer");
-    const int st = scan_tiles(P);
-    if ((e = c->scan.ensure((size_t)st * NCNT * sizeof(unsigned long long) + 64)) != cudaSuccess)
-        return cuda_fail(c, e, "scan buffer");
+    const size_t sb = (scan_scratch_bytes(P) + 255) / 256 * 256;
+    if ((e = c->scan.ensure(sb + 64)) != cudaSuccess) return cuda_fail(c, e, "scan buffer");
     P.cnt = (uint32_t *)c->cnt.ptr;
     P.base = (int64_t *)c->base.ptr;
     P.flags = (uint8_t *)c->flags.ptr;
     P.scan_state = (unsigned long long *)c->scan.ptr;
-    P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + (size_t)st * NCNT * sizeof(unsigned long long));
+    P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + sb);
     // misc: totals[NCNT] int64, then the error word, the work counter and the
     // staging counter
     P.totals = (int64_t *)c->misc.ptr;

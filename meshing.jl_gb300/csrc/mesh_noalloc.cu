@@ -30,7 +30,7 @@
 namespace mesh {
 cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStream_t s);
 cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
-int scan_tiles(const Plan &p);
+size_t scan_scratch_bytes(const Plan &p);
 }  // namespace mesh
 
 using namespace mesh;
@@ -133,13 +133,13 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     // scratch layout inside g_scratch (each array 256-byte aligned)
     const int64_t ntab = nx + ny + nz;
     const int64_t np = npieces(P);
-    const int st = scan_tiles(P);
+    const size_t sb = (scan_scratch_bytes(P) + 255) / 256 * 256;
     const size_t es = dtype_size(T);
     const int64_t cap = prm->alg == MESH_ALG_MC ? verts_cap / 3 : 0;  // active MC cells emit >= 3 vertices
     const int64_t nside = cap / ENT_BLOCK + 1;
     size_t off = 0;
     const size_t o_misc = off;   off += up256((NCNT + 2) * sizeof(int64_t));
-    const size_t o_scan = off;   off += up256((size_t)st * NCNT * 8 + 64);
+    const size_t o_scan = off;   off += up256(sb + 64);
     const size_t o_tab = off;    off += up256(table_bytes(ntab));
     const size_t o_cnt = off;    off += up256((size_t)np * NCNT * 4);
     const size_t o_base = off;   off += up256((size_t)np * NCNT * 8);
@@ -156,7 +156,7 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     P.err = (unsigned int *)((int64_t *)(base + o_misc) + NCNT);
     P.work = (unsigned int *)((int64_t *)(base + o_misc) + NCNT + 1);
     P.scan_state = (unsigned long long *)(base + o_scan);
-    P.scan_ticket = (unsigned int *)(base + o_scan + (size_t)st * NCNT * 8);
+    P.scan_ticket = (unsigned int *)(base + o_scan + sb);
     double *dp = (double *)(base + o_tab);
     bind_tables(P, dp, nx, ny, nz);
     P.pstride = np;
