@@ -38,7 +38,8 @@ typedef enum {
     MESH_DT_F32 = 2, /* Float32 */
     MESH_DT_F64 = 3, /* Float64 */
     MESH_DT_I64 = 4, /* Int64 */
-    MESH_DT_I32 = 5  /* Int32 (volumes only) */
+    MESH_DT_I32 = 5, /* Int32 (volumes only) */
+    MESH_DT_F16 = 6  /* Float16 (volumes only; iso of type Float32 or Float64) */
 } mesh_dtype;
 
 typedef enum {
@@ -66,7 +67,7 @@ typedef enum {
  * with its Julia type; Int64 values must satisfy |v| <= 2^53. */
 typedef struct {
     int32_t alg;        /* mesh_alg */
-    int32_t iso_type;   /* MESH_DT_F32 | MESH_DT_F64 | MESH_DT_I64 */
+    int32_t iso_type;   /* MESH_DT_F32 | MESH_DT_F64 | MESH_DT_I64 (not I64 with MESH_DT_F16 volumes) */
     double iso;
     int32_t eps_type;   /* MESH_DT_F32 | MESH_DT_F64 (MT only; ignored otherwise) */
     double eps;

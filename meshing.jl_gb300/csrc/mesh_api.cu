@@ -81,8 +81,12 @@ int out_is_f64(const int *tys, int n) {
 
 int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_params *p) {
     if (!p) return fail(c, MESH_EINVAL, "params is NULL");
-    if (T != MESH_DT_U16 && T != MESH_DT_F32 && T != MESH_DT_F64 && T != MESH_DT_I32 && T != MESH_DT_I64)
+    if (T != MESH_DT_U16 && T != MESH_DT_F32 && T != MESH_DT_F64 && T != MESH_DT_I32 && T != MESH_DT_I64 &&
+        T != MESH_DT_F16)
         return fail(c, MESH_EINVAL, "unsupported volume dtype %d", T);
+    // promote(Int, Float16) is Float16: (iso - v1) / (v2 - v1) would run in Float16 arithmetic
+    if (T == MESH_DT_F16 && p && p->iso_type == MESH_DT_I64)
+        return fail(c, MESH_EINVAL, "Float16 volumes take a Float32 or Float64 iso");
     if (p->alg != MESH_ALG_MC && p->alg != MESH_ALG_MT && p->alg != MESH_ALG_NSN)
         return fail(c, MESH_EINVAL, "unknown algorithm %d", p->alg);
     if (p->iso_type != MESH_DT_F32 && p->iso_type != MESH_DT_F64 && p->iso_type != MESH_DT_I64)
@@ -304,7 +308,7 @@ bool make_tensor_map(mesh_ctx *c) {
     case MESH_DT_U16: bx = TmaBox<uint16_t>::BX; es = 2; dt = CU_TENSOR_MAP_DATA_TYPE_UINT16; break;
     case MESH_DT_F32: bx = TmaBox<float>::BX; es = 4; dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; break;
     case MESH_DT_F64: bx = TmaBox<double>::BX; es = 8; dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; break;
-    default: return false;  // integer volumes take the load walk
+    default: return false;  // integer and Float16 volumes take the load walk
     }
     if (((uintptr_t)P.vol & 15) || ((size_t)P.nx * es) % 16 || P.nx < bx || P.ny < TMA_BY || P.nz < TMA_BZ) return false;
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();

@@ -1,6 +1,7 @@
 // Internal definitions shared by the host runtime (mesh_api.cu) and the
 // kernels (k_*.cu).  Not part of the public ABI.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -127,7 +128,7 @@ struct BatchVol {
 
 // Bytes per sample of a volume dtype.
 inline __host__ __device__ size_t dtype_size(int T) {
-    return T == MESH_DT_U16 ? 2 : (T == MESH_DT_F32 || T == MESH_DT_I32) ? 4 : 8;
+    return (T == MESH_DT_U16 || T == MESH_DT_F16) ? 2 : (T == MESH_DT_F32 || T == MESH_DT_I32) ? 4 : 8;
 }
 
 inline __host__ __device__ int64_t npieces(const Plan &p) { return (int64_t)p.nseg * p.cy * p.cx; }
@@ -229,7 +230,18 @@ template <> struct Ar<double> {
     static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
 };
 
+// A Float16 sample, kept as its IEEE binary16 bits.  Every Float16 value is a
+// Float32 value, so it converts exactly; T(0) is the zero sample.
+struct h16 {
+    uint16_t b;
+    h16() = default;
+    __host__ __device__ constexpr explicit h16(int) : b(0) {}
+    __device__ __forceinline__ operator float() const { return __half2float(__ushort_as_half(b)); }
+};
+static_assert(sizeof(h16) == 2, "binary16 storage");
+
 // v < iso, exact, in the data type.
+__device__ __forceinline__ bool below(h16 v, const Plan &p) { return (float)v < p.thr_f; }
 __device__ __forceinline__ bool below(float v, const Plan &p) { return v < p.thr_f; }
 __device__ __forceinline__ bool below(double v, const Plan &p) { return v < p.thr_d; }
 __device__ __forceinline__ bool below(uint16_t v, const Plan &p) { return (int32_t)v < p.thr_i; }
@@ -238,6 +250,11 @@ __device__ __forceinline__ bool below(int64_t v, const Plan &p) { return v < p.t
 
 // v2 - v1 in the data type (UInt16 wraps), then converted to Q.
 template <class Q> __device__ __forceinline__ Q tdiff(float v2, float v1) { return (Q)__fsub_rn(v2, v1); }
+// Float16 - Float16 is a Float16: the Float32 difference of two Float16 values
+// is exact, so rounding it to Float16 once gives the IEEE half subtraction.
+template <class Q> __device__ __forceinline__ Q tdiff(h16 v2, h16 v1) {
+    return (Q)__half2float(__float2half_rn(__fsub_rn((float)v2, (float)v1)));
+}
 template <class Q> __device__ __forceinline__ Q tdiff(double v2, double v1) { return (Q)__dsub_rn(v2, v1); }
 template <class Q> __device__ __forceinline__ Q tdiff(uint16_t v2, uint16_t v1) { return (Q)(uint16_t)(v2 - v1); }
 // machine-integer differences wrap; the conversion to Q rounds to nearest
@@ -305,11 +322,21 @@ __device__ __forceinline__ bool fast_f32_pos(float mu, float p1h, float p1l, flo
 }
 
 template <class T> __device__ __forceinline__ T shfl_down1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+template <> __device__ __forceinline__ h16 shfl_down1<h16>(h16 v) {
+    h16 r;
+    r.b = (uint16_t)__shfl_down_sync(0xffffffffu, (unsigned)v.b, 1);
+    return r;
+}
 template <> __device__ __forceinline__ uint16_t shfl_down1<uint16_t>(uint16_t v) {
     return (uint16_t)__shfl_down_sync(0xffffffffu, (unsigned)v, 1);
 }
 
 template <class T> __device__ __forceinline__ T ldv(const T *p) { return __ldg(p); }
+template <> __device__ __forceinline__ h16 ldv<h16>(const h16 *p) {
+    h16 r;
+    r.b = __ldg(reinterpret_cast<const unsigned short *>(p));
+    return r;
+}
 template <> __device__ __forceinline__ uint16_t ldv<uint16_t>(const uint16_t *p) {
     return __ldg(reinterpret_cast<const unsigned short *>(p));
 }

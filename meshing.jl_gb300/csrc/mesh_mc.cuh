@@ -171,7 +171,24 @@ template <> __device__ __forceinline__ void store8<int64_t>(int64_t *dst, const 
 #pragma unroll
     for (int k = 0; k < 4; k++) d[k] = make_longlong2(v[2 * k], v[2 * k + 1]);
 }
+template <> __device__ __forceinline__ void store8<h16>(h16 *dst, const h16 (&v)[8]) {
+    uint4 q;
+    q.x = v[0].b | (uint32_t)v[1].b << 16;
+    q.y = v[2].b | (uint32_t)v[3].b << 16;
+    q.z = v[4].b | (uint32_t)v[5].b << 16;
+    q.w = v[6].b | (uint32_t)v[7].b << 16;
+    *reinterpret_cast<uint4 *>(dst) = q;
+}
 template <class T> __device__ __forceinline__ void load8(const T *src, T (&v)[8]);
+template <> __device__ __forceinline__ void load8<h16>(const h16 *src, h16 (&v)[8]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(src);
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[2 * k].b = (uint16_t)(w[k] & 0xffffu);
+        v[2 * k + 1].b = (uint16_t)(w[k] >> 16);
+    }
+}
 template <> __device__ __forceinline__ void load8<int32_t>(const int32_t *src, int32_t (&v)[8]) {
     const int4 a = reinterpret_cast<const int4 *>(src)[0], b = reinterpret_cast<const int4 *>(src)[1];
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;

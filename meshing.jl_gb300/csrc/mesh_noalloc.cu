@@ -31,6 +31,7 @@ namespace mesh {
 cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStream_t s);
 cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
 size_t scan_scratch_bytes(const Plan &p);
+void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P64);
 }  // namespace mesh
 
 using namespace mesh;
@@ -87,40 +88,11 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
     P.vol = vol;
     P.nx = nx; P.ny = ny; P.nz = nz;
     P.cx = (int32_t)(nx - 1); P.cy = (int32_t)(ny - 1); P.cz = (int32_t)(nz - 1);
-    P.T = T;
-    P.alg = prm->alg;
-    const int I = prm->iso_type, E = prm->eps_type, Rt = prm->range_type;
-    const int mt = prm->alg == MESH_ALG_MT;
-    const int Q64 = T == MESH_DT_F64 || I == MESH_DT_F64 || (T == MESH_DT_U16 && I == MESH_DT_I64);
-    const int L32 = Rt == MESH_DT_F32;
-    const int A64 = mt ? (Q64 || E == MESH_DT_F64) : Q64;
-    const int P64 = (mt ? A64 : Q64) || !L32;
-    P.out64 = bits == 64;
-    const double iso = prm->iso;
-    float f = (float)iso;
-    if (!std::isnan(iso) && (double)f < iso) f = std::nextafter(f, INFINITY);
-    P.thr_f = f;
-    P.thr_d = iso;
-    P.thr_i = (int32_t)std::min(65536.0, std::max(0.0, std::isnan(iso) ? 0.0 : std::ceil(iso)));
-    P.isoq_d = iso;
-    P.isoq_f = (float)iso;
-    if (mt) {
-        const int te64 = T == MESH_DT_F64 || E == MESH_DT_F64;
-        const double hi = te64 ? 1.0 - prm->eps : (double)(1.0f - (float)prm->eps);
-        P.eps_d = prm->eps; P.hi_d = hi;
-        P.eps_f = (float)prm->eps; P.hi_f = (float)hi;
-        for (int bnd = 0; bnd < 8; bnd++) {
-            uint32_t m = 0;
-            for (int ed = 0; ed < 19; ed++) {
-                const int i1 = MT_EDGE_CORNERS[ed][0], i2 = MT_EDGE_CORNERS[ed][1];
-                int za = 0;
-                for (int k = 0; k < 3; k++)
-                    if (MT_CORNER_POS[i1][k] == 0 && MT_CORNER_POS[i2][k] == 0) za |= 1 << k;
-                if ((za & ~bnd) == 0) m |= 1u << ed;
-            }
-            P.own[bnd] = m;
-        }
-    }
+    // types, thresholds and MT clamps exactly as the context path sets them
+    int Q64 = 0, A64 = 0, P64 = 0;
+    set_types(P, T, prm, &Q64, &A64, &P64);
+    const int L32 = prm->range_type == MESH_DT_F32;
+    if (P.out64 != (bits == 64)) return MESH_EINVAL;
     // one z segment per column keeps the per-piece scratch small
     P.tiles_x = (P.cx + TILE_X - 1) / TILE_X;
     P.tiles_y = (P.cy + WY - 1) / WY;

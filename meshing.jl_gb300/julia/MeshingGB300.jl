@@ -4,11 +4,12 @@
 Drop-in GPU back end for Meshing.jl.  Loading this module adds methods of
 `Meshing.isosurface` that are more specific than the reference's
 (src/marching_cubes.jl:27, src/marching_tetrahedra.jl:129): dense
-`Array{T,3}` volumes with `T ∈ {UInt16, Int32, Int64, Float32, Float64}` and iso / eps /
-range endpoints of type Float32, Float64 or Int64 run on the GPU through
-`libmeshing_gb300.so`.  Every other combination (Float16, Int data,
-ForwardDiff.Dual, mixed endpoint types) reaches the reference method through
-`invoke`, i.e. ordinary dispatch, not a fallback inside the library.
+`Array{T,3}` volumes with `T ∈ {UInt16, Int32, Int64, Float16, Float32, Float64}` and
+iso / eps / range endpoints of type Float32, Float64 or Int64 run on the GPU through
+`libmeshing_gb300.so` (Float16 data with a Float32 or Float64 iso).  Every other
+combination (Float16 data with an Int iso, Int8/Int16 data, ForwardDiff.Dual,
+mixed endpoint types) reaches the reference method through `invoke`, i.e.
+ordinary dispatch, not a fallback inside the library.
 Results are identical to the reference's: the same element types, vertex
 order and 1-based faces.  `NaiveSurfaceNets` (named in the reference's README
 but not implemented there) is added with the definition documented in the
@@ -44,7 +45,7 @@ struct MeshParams
     range::NTuple{6,Float64}
 end
 
-const DevEl = Union{UInt16,Int32,Int64,Float32,Float64}
+const DevEl = Union{UInt16,Int32,Int64,Float16,Float32,Float64}
 const DevScalar = Union{Float32,Float64,Int64}
 
 dtcode(::Type{UInt16}) = Int32(1)
@@ -52,6 +53,9 @@ dtcode(::Type{Float32}) = Int32(2)
 dtcode(::Type{Float64}) = Int32(3)
 dtcode(::Type{Int64}) = Int32(4)
 dtcode(::Type{Int32}) = Int32(5)
+dtcode(::Type{Float16}) = Int32(6)
+# promote(Int, Float16) is Float16: that quotient runs in Float16 arithmetic, left to the reference
+device_ok(::Type{T}, ::Type{I}) where {T,I} = !(T === Float16 && I === Int64)
 dtcode(::Type) = Int32(0)
 
 # one context per thread: a context is not thread-safe
@@ -102,21 +106,24 @@ function device_isosurface(sdf::Array{T,3}, alg::Int32, iso, eps, X, Y, Z, ::Typ
 end
 
 function isosurface(sdf::Array{T,3}, method::MarchingCubes{I}, X=-1:1, Y=-1:1, Z=-1:1) where {T<:DevEl,I<:DevScalar}
-    supported(X, Y, Z) || return invoke(isosurface, Tuple{AbstractArray{T,3},MarchingCubes,typeof(X),typeof(Y),typeof(Z)},
-                                        sdf, method, X, Y, Z)
+    (supported(X, Y, Z) && device_ok(T, I)) ||
+        return invoke(isosurface, Tuple{AbstractArray{T,3},MarchingCubes,typeof(X),typeof(Y),typeof(Z)},
+                      sdf, method, X, Y, Z)
     FT = promote_type(eltype(first(X)), eltype(first(Y)), eltype(first(Z)), T, I)
     device_isosurface(sdf, Int32(0), method.iso, 1e-3, X, Y, Z, float(FT))
 end
 
 function isosurface(sdf::Array{T,3}, method::MarchingTetrahedra{I,E}, X=-1:1, Y=-1:1, Z=-1:1) where {T<:DevEl,I<:DevScalar,E<:Union{Float32,Float64}}
-    supported(X, Y, Z) || return invoke(isosurface, Tuple{AbstractArray{T,3},MarchingTetrahedra,typeof(X),typeof(Y),typeof(Z)},
-                                        sdf, method, X, Y, Z)
+    (supported(X, Y, Z) && device_ok(T, I)) ||
+        return invoke(isosurface, Tuple{AbstractArray{T,3},MarchingTetrahedra,typeof(X),typeof(Y),typeof(Z)},
+                      sdf, method, X, Y, Z)
     FT = promote_type(eltype(first(X)), eltype(first(Y)), eltype(first(Z)), T, I, E)
     device_isosurface(sdf, Int32(1), method.iso, method.eps, X, Y, Z, float(FT))
 end
 
 function isosurface(sdf::Array{T,3}, method::NaiveSurfaceNets{I}, X=-1:1, Y=-1:1, Z=-1:1) where {T<:DevEl,I<:DevScalar}
     supported(X, Y, Z) || error("NaiveSurfaceNets: range endpoints must share one of Float32, Float64, Int64")
+    device_ok(T, I) || error("NaiveSurfaceNets: Float16 volumes take a Float32 or Float64 iso")
     FT = promote_type(eltype(first(X)), eltype(first(Y)), eltype(first(Z)), T, I)
     device_isosurface(sdf, Int32(2), method.iso, 1e-3, X, Y, Z, float(FT))
 end

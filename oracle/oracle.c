@@ -37,7 +37,7 @@
 
 #include "ref_luts.h"
 
-enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4, ORC_I32 = 5 };
+enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4, ORC_I32 = 5, ORC_F16 = 6 };
 enum { ORC_MC = 0, ORC_MT = 1, ORC_NSN = 2 };
 enum { ORC_OK = 0, ORC_EINVAL = 1, ORC_ENOMEM = 2 };
 
@@ -94,10 +94,23 @@ static int64_t unpun(double d) {
     return i;
 }
 
+/* IEEE binary16 bits -> the value (exact in double). */
+static double half_value(uint16_t h) {
+    const int s = h >> 15, e = (h >> 10) & 31, m = h & 1023;
+    double v;
+    if (e == 0) v = ldexp((double)m, -24);                 /* zero, subnormal */
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = ldexp((double)(m | 1024), e - 25);
+    return s ? -v : v;
+}
+/* x rounded to the nearest binary16 (ties to even): Float16(x) in Julia. */
+static double round_half(double x) { return (double)(_Float16)x; }
+
 static double load(const orc_ctx *c, int64_t x, int64_t y, int64_t z) {
     int64_t i = x + c->nx * (y + c->ny * z);
     switch (c->T) {
     case ORC_U16: return (double)((const uint16_t *)c->vol)[i];
+    case ORC_F16: return half_value(((const uint16_t *)c->vol)[i]);
     case ORC_F32: return (double)((const float *)c->vol)[i];
     case ORC_I32: return pun((int64_t)((const int32_t *)c->vol)[i]);
     case ORC_I64: return pun(((const int64_t *)c->vol)[i]);
@@ -142,6 +155,8 @@ static double quotient(const orc_ctx *c, double v1, double v2) {
         den = (double)(uint16_t)((uint16_t)v2 - (uint16_t)v1); /* UInt16 wraps */
     else if (c->T == ORC_F32)
         den = rnd(ORC_F32, v2 - v1);
+    else if (c->T == ORC_F16)
+        den = round_half(v2 - v1); /* Float16 - Float16: the exact difference, rounded once */
     else
         den = v2 - v1;
     if (c->Q == ORC_F32) {
@@ -461,7 +476,8 @@ static int run_nsn(const orc_ctx *c, orc_mesh *m) {
 static int setup(orc_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int alg, int I, double iso,
                  int E, double eps, int R, const double *rg) {
     memset(c, 0, sizeof(*c));
-    if (T != ORC_U16 && T != ORC_F32 && T != ORC_F64 && T != ORC_I32 && T != ORC_I64) return ORC_EINVAL;
+    if (T != ORC_U16 && T != ORC_F32 && T != ORC_F64 && T != ORC_I32 && T != ORC_I64 && T != ORC_F16) return ORC_EINVAL;
+    if (T == ORC_F16 && I == ORC_I64) return ORC_EINVAL; /* promote(Int, Float16): Float16 arithmetic, not restated */
     if (I != ORC_F32 && I != ORC_F64 && I != ORC_I64) return ORC_EINVAL;
     if (R != ORC_F32 && R != ORC_F64 && R != ORC_I64) return ORC_EINVAL;
     if (alg == ORC_MT && E != ORC_F32 && E != ORC_F64) return ORC_EINVAL;

@@ -44,6 +44,8 @@ def _promote(*tys):
         return np.float64
     if np.float32 in tys:
         return np.float32
+    if np.float16 in tys:  # promote(Float16, Int) is Float16
+        return np.float16
     if np.int64 in tys:
         return np.int64
     if np.int32 in tys:

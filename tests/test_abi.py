@@ -44,6 +44,10 @@ def test_params_default_mirror_reference(pkg):
     (np.float32, ('mt', np.float32(0), np.float32(1e-3)), (-1, 1), 32),
     (np.float32, ('mt', np.float32(0), 1e-3), (-1, 1), 64),
     (np.float32, ('nsn', np.float32(0)), (-1, 1), 32),
+    (np.float16, ('mc', 0.0), (-1, 1), 64),
+    (np.float16, ('mc', np.float32(0)), (-1, 1), 32),
+    (np.float16, ('mc', np.float32(0)), (-1.0, 1.0), 64),
+    (np.float16, ('mt', np.float32(0), np.float32(1e-3)), (np.float32(0), np.float32(1)), 32),
 ])
 def test_output_eltype_matches_oracle(pkg, oracle, dtype, method, rng, bits):
     alg = method[0]
@@ -71,6 +75,11 @@ def test_invalid_arguments_rejected(pkg):
     p.iso = 0.1  # not a Float32 value
     assert pkg.load_library().mesh_output_float_bits(2, ctypes.byref(p), ctypes.byref(bits)) == 1
     assert pkg.load_library().mesh_output_float_bits(9, ctypes.byref(p), ctypes.byref(bits)) == 1
+    # Float16 data with an Int iso would divide in Float16 arithmetic: not taken
+    p = pkg.make_params(pkg.MarchingCubes(iso=0))
+    assert pkg.load_library().mesh_output_float_bits(6, ctypes.byref(p), ctypes.byref(bits)) == 1
+    p = pkg.make_params(pkg.MarchingCubes(iso=np.float32(0)))
+    assert pkg.load_library().mesh_output_float_bits(6, ctypes.byref(p), ctypes.byref(bits)) == 0
 
 
 def test_generic_forwarder_defaults_to_marching_cubes(pkg):

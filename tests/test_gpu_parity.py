@@ -91,6 +91,10 @@ TYPE_CASES = [
     (np.uint16, 500, np.float32(1e-3), (np.float32(0), np.float32(7))),
     (np.uint16, np.float32(300.5), np.float32(1e-3), (-1, 1)),
     (np.uint16, 250.25, 1e-3, (0.0, 1.0)),
+    (np.float16, 0.0, 1e-3, (-1, 1)),
+    (np.float16, np.float32(0.1), np.float32(1e-3), (-1, 1)),
+    (np.float16, np.float32(-0.3), 1e-3, (np.float32(-2), np.float32(3))),
+    (np.float16, 0.25, np.float32(1e-2), (0.0, 1.0)),
 ]
 
 
@@ -245,3 +249,18 @@ def test_integer_field_many_tiles(pkg, oracle, cuda, alg):
     A = (sphere(0, 0.6, np.float64, c=(0.1, 0.0, -0.05), shape=(97, 70, 133)) * 100000).astype(np.int32)
     check(pkg, oracle, A, alg, 0)
     check(pkg, oracle, A, alg, 2500.5, 1e-3, ((0, 1),) * 3, device=True)
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_float16_volumes(pkg, oracle, cuda, alg):
+    # test/runtests.jl:56-65 runs the algorithms on Float16 data.  Float32 / Float64 iso:
+    # exact comparison, v2 - v1 a Float16 subtraction, quotient in promote(typeof(iso), Float16)
+    rng = np.random.default_rng(61 + len(alg))
+    A = sphere(0, 0.6, np.float16, c=(0.05, -0.1, 0.0), shape=(67, 45, 133))  # several x / y tiles, z segments
+    check(pkg, oracle, A, alg, np.float32(0))
+    check(pkg, oracle, A, alg, 0.0, 1e-3, ((0, 1),) * 3, device=True)
+    big = np.clip(rng.standard_normal((23, 17, 29)) * 3e4, -65504, 65504).astype(np.float16)  # differences round / overflow
+    big.ravel(order='K')[:4] = [np.inf, -np.inf, np.nan, np.float16(65504)]
+    for iso in (np.float32(0), 1.0e4, np.float32(-2.5e4)):
+        check(pkg, oracle, big, alg, iso, np.float32(1e-3) if isinstance(iso, np.float32) else 1e-3)
+    check(pkg, oracle, big, alg, 0.0, 1e-3, ((np.float32(-2), np.float32(3)),) * 3, device=True)

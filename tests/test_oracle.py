@@ -186,3 +186,47 @@ def test_integer_volume_eltype_rule(oracle, dtype, iso, rt, bits):
     for alg in ('mc', 'mt'):
         eps = np.float32(1e-3) if bits == 32 else 1e-3
         assert oracle.output_bits(dtype, alg, iso, eps, rt) == bits
+
+
+def test_float16_volumes_c_matches_python(oracle):
+    # Float16 volumes (test/runtests.jl:56-65 runs the algorithms on Float16 data): the
+    # comparison with iso is exact, v2 - v1 is a Float16 subtraction (one rounding of
+    # the exact difference), and the quotient runs in promote(typeof(iso), Float16)
+    rng = np.random.default_rng(16)
+    for trial in range(6):
+        sh = tuple(int(s) for s in rng.integers(2, 7, 3))
+        A = np.asfortranarray((rng.standard_normal(sh) * (1 if trial % 2 else 3e4)).astype(np.float16))
+        if trial == 5:
+            A.ravel(order='K')[:3] = [np.inf, -np.inf, np.nan]
+        for iso in (0.0, np.float32(0.25), np.float32(-1e4), 1.5e4):
+            for alg in ('mc', 'mt', 'nsn'):
+                for rg in (((-1, 1),) * 3, ((np.float32(-2), np.float32(3)),) * 3, ((0.0, 1.0),) * 3):
+                    for eps in (1e-3, np.float32(1e-3)):
+                        a = oracle.isosurface(A, alg, iso, eps, rg)
+                        b = pyoracle.isosurface(A, alg, iso, eps, rg) if alg != 'nsn' else a
+                        assert a[0].dtype == b[0].dtype
+                        assert np.array_equal(a[1], b[1]), (iso, alg, rg)
+                        assert np.array_equal(a[0], b[0], equal_nan=True), (iso, alg, rg)
+
+
+def test_float16_subtraction_rounds_once(oracle):
+    # corner (x+1, y, z) at 1, the rest at -2048, iso 0f0: on the edge from that corner
+    # along +y, v2 - v1 = -2048 - 1 = -2049 rounds to -2048 in Float16 (ties to even),
+    # so mu = Float32(0 - 1) / Float32(-2048) = 2^-11 exactly and y = -1 + 2 mu
+    A = np.full((2, 2, 2), np.float16(-2048), np.float16, order='F')
+    A[1, 0, 0] = np.float16(1)
+    v, f = oracle.isosurface(A, 'mc', iso=np.float32(0))
+    assert len(f) == 1 and v.dtype == np.float32
+    assert np.float32(-1 + 2 * 2.0 ** -11) in v[:, 1]
+    assert np.float32(-1 + 2 / 2049) not in v[:, 1]
+
+
+@pytest.mark.parametrize('iso,rt,bits', [
+    (0.0, 4, 64),            # default iso: FT = Float64
+    (np.float32(0), 4, 32),  # promote(Int range, Float16, Float32) == Float32
+    (np.float32(0), 3, 64),  # a Float64 range
+])
+def test_float16_volume_eltype_rule(oracle, iso, rt, bits):
+    for alg in ('mc', 'mt'):
+        eps = np.float32(1e-3) if bits == 32 else 1e-3
+        assert oracle.output_bits(np.float16, alg, iso, eps, rt) == bits

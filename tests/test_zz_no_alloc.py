@@ -32,7 +32,7 @@ def _volume(torch, shape, kind, dtype):
 def _run_both(pkg, torch, vol, method, ranges):
     lib = pkg.load_library()
     p = pkg.make_params(method, *ranges)
-    dt = {torch.float32: 2, torch.float64: 3}[vol.dtype]
+    dt = pkg._lib.torch_dtype_code(vol.dtype)
     nx, ny, nz = vol.shape
     ref_counts = pkg.isosurface_device(vol, method, *ranges,
                                        verts=torch.empty((1, 3), device='cuda'),
@@ -42,7 +42,9 @@ def _run_both(pkg, torch, vol, method, ranges):
     except pkg.MeshError:
         pass  # capacity 1: only the counts are wanted here
     nv, nf = ref_counts.tolist()
-    bits = pkg.output_float_bits(np.float32 if vol.dtype == torch.float32 else np.float64, method, *ranges)
+    npdt = {torch.float32: np.float32, torch.float64: np.float64, torch.int32: np.int32, torch.int64: np.int64,
+            torch.uint16: np.uint16}[vol.dtype]
+    bits = pkg.output_float_bits(npdt, method, *ranges)
     ft = torch.float32 if bits == 32 else torch.float64
     rv = torch.empty((nv, 3), dtype=ft, device='cuda')
     rf = torch.empty((nf, 3), dtype=torch.int64, device='cuda')
@@ -82,6 +84,26 @@ def test_noalloc_matches_allocating_entry_point_on_consecutive_calls(pkg, cuda):
     assert all(nv > 0 and nf > 0 for nv, nf in sizes)
     # the same call twice in a row gives the same answer
     assert _run_both(pkg, torch, *calls[0]) == sizes[0]
+
+
+def test_noalloc_integer_and_uint16_volumes(pkg, cuda):
+    # the integer-vs-iso thresholds and Int / Int quotients of the context path
+    torch = cuda
+    base = _volume(torch, (47, 52, 45), 'sphere', torch.float64)
+    i32 = (base * 1000).round().to(torch.int32)
+    i64 = (base * 3e15).round().to(torch.int64)
+    u = np.round((base.cpu().numpy() + 1) * 20000).astype(np.uint16)  # Julia layout, as base
+    u16 = torch.from_numpy(np.ascontiguousarray(u.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+    calls = [
+        (i32, pkg.MarchingCubes(iso=7), ((-1, 1),) * 3),
+        (i64, pkg.MarchingCubes(iso=12345), ((0, 1),) * 3),
+        (i32, pkg.MarchingTetrahedra(iso=-3), ((-1, 1),) * 3),
+        (u16, pkg.MarchingCubes(iso=20500), ((-1, 1),) * 3),
+        (u16, pkg.NaiveSurfaceNets(iso=np.float32(20000.5)), ((-1, 1),) * 3),
+    ]
+    for c in calls:
+        nv, nf = _run_both(pkg, torch, *c)
+        assert nv > 0 and nf > 0
 
 
 def test_noalloc_rejects_calls_beyond_its_scratch(pkg, cuda):
