@@ -39,7 +39,10 @@ typedef enum {
     MESH_DT_F64 = 3, /* Float64 */
     MESH_DT_I64 = 4, /* Int64 */
     MESH_DT_I32 = 5, /* Int32 (volumes only) */
-    MESH_DT_F16 = 6  /* Float16 (volumes only; iso of type Float32 or Float64) */
+    MESH_DT_F16 = 6, /* Float16 (volumes only; iso of type Float32 or Float64) */
+    MESH_DT_I16 = 7, /* Int16 (volumes only) */
+    MESH_DT_I8 = 8,  /* Int8 (volumes only) */
+    MESH_DT_U8 = 9   /* UInt8 (volumes only) */
 } mesh_dtype;
 
 typedef enum {

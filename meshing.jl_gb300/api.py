@@ -20,7 +20,8 @@ from typing import Any
 import numpy as np
 
 from . import _lib
-from ._lib import (MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN, MESH_DT_F16, MESH_DT_F32, MESH_DT_F64, MESH_DT_I32, MESH_DT_I64, MESH_DT_U16,
+from ._lib import (MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN, MESH_DT_F16, MESH_DT_F32, MESH_DT_F64, MESH_DT_I8, MESH_DT_I16,
+                   MESH_DT_I32, MESH_DT_I64, MESH_DT_U8, MESH_DT_U16,
                    Context, MeshParams, check)
 
 
@@ -56,7 +57,8 @@ class NaiveSurfaceNets(AbstractMeshingAlgorithm):
 
 _ALG = {MarchingCubes: MESH_ALG_MC, MarchingTetrahedra: MESH_ALG_MT, NaiveSurfaceNets: MESH_ALG_NSN}
 _VOL_DT = {np.dtype(np.uint16): MESH_DT_U16, np.dtype(np.float32): MESH_DT_F32, np.dtype(np.float64): MESH_DT_F64,
-           np.dtype(np.int32): MESH_DT_I32, np.dtype(np.int64): MESH_DT_I64, np.dtype(np.float16): MESH_DT_F16}
+           np.dtype(np.int32): MESH_DT_I32, np.dtype(np.int64): MESH_DT_I64, np.dtype(np.float16): MESH_DT_F16,
+           np.dtype(np.int16): MESH_DT_I16, np.dtype(np.int8): MESH_DT_I8, np.dtype(np.uint8): MESH_DT_U8}
 
 
 def _scalar(v, what):

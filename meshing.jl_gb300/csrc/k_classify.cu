@@ -616,6 +616,9 @@ cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: fn = (const void *)k_classify_batch<uint16_t>; break;
     case MESH_DT_F16: fn = (const void *)k_classify_batch<h16>; break;
+    case MESH_DT_I16: fn = (const void *)k_classify_batch<int16_t>; break;
+    case MESH_DT_I8: fn = (const void *)k_classify_batch<int8_t>; break;
+    case MESH_DT_U8: fn = (const void *)k_classify_batch<uint8_t>; break;
     case MESH_DT_F32: fn = (const void *)k_classify_batch<float>; break;
     case MESH_DT_I32: fn = (const void *)k_classify_batch<int32_t>; break;
     case MESH_DT_I64: fn = (const void *)k_classify_batch<int64_t>; break;
@@ -626,6 +629,9 @@ cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: k_classify_batch<uint16_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_DT_F16: k_classify_batch<h16><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    case MESH_DT_I16: k_classify_batch<int16_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    case MESH_DT_I8: k_classify_batch<int8_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
+    case MESH_DT_U8: k_classify_batch<uint8_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_DT_F32: k_classify_batch<float><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_DT_I32: k_classify_batch<int32_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_DT_I64: k_classify_batch<int64_t><<<grid, 32 * WARPS, 0, s>>>(p); break;
@@ -638,6 +644,9 @@ cudaError_t launch_classify(const Plan &p, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: return launch_t<uint16_t>(p, s);
     case MESH_DT_F16: return launch_t<h16>(p, s);
+    case MESH_DT_I16: return launch_t<int16_t>(p, s);
+    case MESH_DT_I8: return launch_t<int8_t>(p, s);
+    case MESH_DT_U8: return launch_t<uint8_t>(p, s);
     case MESH_DT_F32: return launch_t<float>(p, s);
     case MESH_DT_I32: return launch_t<int32_t>(p, s);
     case MESH_DT_I64: return launch_t<int64_t>(p, s);

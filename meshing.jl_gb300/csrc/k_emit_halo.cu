@@ -478,6 +478,9 @@ cudaError_t launch_emit_halo(const Plan &p, int Q64, int A64, int P64, cudaStrea
     switch (p.T) {
     case MESH_DT_U16: return go_t<uint16_t>(p, Q64, A64, P64, s);
     case MESH_DT_F16: return go_t<h16>(p, Q64, A64, P64, s);
+    case MESH_DT_I16: return go_t<int16_t>(p, Q64, A64, P64, s);
+    case MESH_DT_I8: return go_t<int8_t>(p, Q64, A64, P64, s);
+    case MESH_DT_U8: return go_t<uint8_t>(p, Q64, A64, P64, s);
     case MESH_DT_F32: return go_t<float>(p, Q64, A64, P64, s);
     case MESH_DT_I32: return go_t<int32_t>(p, Q64, A64, P64, s);
     case MESH_DT_I64: return go_t<int64_t>(p, Q64, A64, P64, s);

@@ -309,6 +309,9 @@ cudaError_t launch_compact_batch(const Plan &p, int ctas, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: return compact_batch_t<uint16_t>(p, ctas, s);
     case MESH_DT_F16: return compact_batch_t<h16>(p, ctas, s);
+    case MESH_DT_I16: return compact_batch_t<int16_t>(p, ctas, s);
+    case MESH_DT_I8: return compact_batch_t<int8_t>(p, ctas, s);
+    case MESH_DT_U8: return compact_batch_t<uint8_t>(p, ctas, s);
     case MESH_DT_F32: return compact_batch_t<float>(p, ctas, s);
     case MESH_DT_I32: return compact_batch_t<int32_t>(p, ctas, s);
     case MESH_DT_I64: return compact_batch_t<int64_t>(p, ctas, s);
@@ -320,6 +323,9 @@ cudaError_t launch_expand_batch(const Plan &p, int Q64, int P64, cudaStream_t s)
     switch (p.T) {
     case MESH_DT_U16: return expand_batch_tt<uint16_t>(p, Q64, P64, s);
     case MESH_DT_F16: return expand_batch_tt<h16>(p, Q64, P64, s);
+    case MESH_DT_I16: return expand_batch_tt<int16_t>(p, Q64, P64, s);
+    case MESH_DT_I8: return expand_batch_tt<int8_t>(p, Q64, P64, s);
+    case MESH_DT_U8: return expand_batch_tt<uint8_t>(p, Q64, P64, s);
     case MESH_DT_F32: return expand_batch_tt<float>(p, Q64, P64, s);
     case MESH_DT_I32: return expand_batch_tt<int32_t>(p, Q64, P64, s);
     case MESH_DT_I64: return expand_batch_tt<int64_t>(p, Q64, P64, s);
@@ -332,6 +338,9 @@ cudaError_t launch_emit_mc(const Plan &p, int Q64, int P64, int stage, cudaStrea
     switch (p.T) {
     case MESH_DT_U16: return go_t<uint16_t>(p, Q64, P64, stage, s);
     case MESH_DT_F16: return go_t<h16>(p, Q64, P64, stage, s);
+    case MESH_DT_I16: return go_t<int16_t>(p, Q64, P64, stage, s);
+    case MESH_DT_I8: return go_t<int8_t>(p, Q64, P64, stage, s);
+    case MESH_DT_U8: return go_t<uint8_t>(p, Q64, P64, stage, s);
     case MESH_DT_F32: return go_t<float>(p, Q64, P64, stage, s);
     case MESH_DT_I32: return go_t<int32_t>(p, Q64, P64, stage, s);
     case MESH_DT_I64: return go_t<int64_t>(p, Q64, P64, stage, s);

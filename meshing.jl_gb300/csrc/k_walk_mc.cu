@@ -211,6 +211,9 @@ cudaError_t launch_walk_mc(const Plan &p, cudaStream_t s) {
     switch (p.T) {
     case MESH_DT_U16: return walk_t<uint16_t>(p, s);
     case MESH_DT_F16: return walk_t<h16>(p, s);
+    case MESH_DT_I16: return walk_t<int16_t>(p, s);
+    case MESH_DT_I8: return walk_t<int8_t>(p, s);
+    case MESH_DT_U8: return walk_t<uint8_t>(p, s);
     case MESH_DT_F32: return walk_t<float>(p, s);
     case MESH_DT_I32: return walk_t<int32_t>(p, s);
     case MESH_DT_I64: return walk_t<int64_t>(p, s);
@@ -222,6 +225,9 @@ cudaError_t launch_expand_staged_mc(const Plan &p, int Q64, int P64, cudaStream_
     switch (p.T) {
     case MESH_DT_U16: return expand_tt<uint16_t>(p, Q64, P64, s);
     case MESH_DT_F16: return expand_tt<h16>(p, Q64, P64, s);
+    case MESH_DT_I16: return expand_tt<int16_t>(p, Q64, P64, s);
+    case MESH_DT_I8: return expand_tt<int8_t>(p, Q64, P64, s);
+    case MESH_DT_U8: return expand_tt<uint8_t>(p, Q64, P64, s);
     case MESH_DT_F32: return expand_tt<float>(p, Q64, P64, s);
     case MESH_DT_I32: return expand_tt<int32_t>(p, Q64, P64, s);
     case MESH_DT_I64: return expand_tt<int64_t>(p, Q64, P64, s);

@@ -82,7 +82,7 @@ int out_is_f64(const int *tys, int n) {
 int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_params *p) {
     if (!p) return fail(c, MESH_EINVAL, "params is NULL");
     if (T != MESH_DT_U16 && T != MESH_DT_F32 && T != MESH_DT_F64 && T != MESH_DT_I32 && T != MESH_DT_I64 &&
-        T != MESH_DT_F16)
+        T != MESH_DT_F16 && T != MESH_DT_I16 && T != MESH_DT_I8 && T != MESH_DT_U8)
         return fail(c, MESH_EINVAL, "unsupported volume dtype %d", T);
     // promote(Int, Float16) is Float16: (iso - v1) / (v2 - v1) would run in Float16 arithmetic
     if (T == MESH_DT_F16 && p && p->iso_type == MESH_DT_I64)
@@ -146,8 +146,8 @@ void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P6
         P.thr_d = iso;
         double ce = std::ceil(iso);
         if (std::isnan(iso)) ce = 0;
-        P.thr_i = (int32_t)std::min(65536.0, std::max(0.0, ce));
-        // Int32 / Int64 data: x < iso  <=>  x < ceil(iso), exact for every Int64 x
+        P.thr_i = (int32_t)std::min(65536.0, std::max(0.0, ce));  // UInt16 / UInt8 data
+        // Int8 / Int16 / Int32 / Int64 data: x < iso  <=>  x < ceil(iso), exact for every Int64 x
         P.thr_all = 0;
         if (std::isnan(iso)) {
             P.thr_l = INT64_MIN;                      // nothing is below NaN

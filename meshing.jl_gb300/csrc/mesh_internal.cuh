@@ -128,7 +128,9 @@ struct BatchVol {
 
 // Bytes per sample of a volume dtype.
 inline __host__ __device__ size_t dtype_size(int T) {
-    return (T == MESH_DT_U16 || T == MESH_DT_F16) ? 2 : (T == MESH_DT_F32 || T == MESH_DT_I32) ? 4 : 8;
+    return (T == MESH_DT_I8 || T == MESH_DT_U8) ? 1
+           : (T == MESH_DT_U16 || T == MESH_DT_F16 || T == MESH_DT_I16) ? 2
+           : (T == MESH_DT_F32 || T == MESH_DT_I32) ? 4 : 8;
 }
 
 inline __host__ __device__ int64_t npieces(const Plan &p) { return (int64_t)p.nseg * p.cy * p.cx; }
@@ -245,6 +247,9 @@ __device__ __forceinline__ bool below(h16 v, const Plan &p) { return (float)v < 
 __device__ __forceinline__ bool below(float v, const Plan &p) { return v < p.thr_f; }
 __device__ __forceinline__ bool below(double v, const Plan &p) { return v < p.thr_d; }
 __device__ __forceinline__ bool below(uint16_t v, const Plan &p) { return (int32_t)v < p.thr_i; }
+__device__ __forceinline__ bool below(uint8_t v, const Plan &p) { return (int32_t)v < p.thr_i; }
+__device__ __forceinline__ bool below(int8_t v, const Plan &p) { return (int64_t)v < p.thr_l || p.thr_all; }
+__device__ __forceinline__ bool below(int16_t v, const Plan &p) { return (int64_t)v < p.thr_l || p.thr_all; }
 __device__ __forceinline__ bool below(int32_t v, const Plan &p) { return (int64_t)v < p.thr_l || p.thr_all; }
 __device__ __forceinline__ bool below(int64_t v, const Plan &p) { return v < p.thr_l || p.thr_all; }
 
@@ -257,6 +262,13 @@ template <class Q> __device__ __forceinline__ Q tdiff(h16 v2, h16 v1) {
 }
 template <class Q> __device__ __forceinline__ Q tdiff(double v2, double v1) { return (Q)__dsub_rn(v2, v1); }
 template <class Q> __device__ __forceinline__ Q tdiff(uint16_t v2, uint16_t v1) { return (Q)(uint16_t)(v2 - v1); }
+template <class Q> __device__ __forceinline__ Q tdiff(uint8_t v2, uint8_t v1) { return (Q)(uint8_t)(v2 - v1); }
+template <class Q> __device__ __forceinline__ Q tdiff(int8_t v2, int8_t v1) {
+    return (Q)(int8_t)(uint8_t)((uint8_t)v2 - (uint8_t)v1);
+}
+template <class Q> __device__ __forceinline__ Q tdiff(int16_t v2, int16_t v1) {
+    return (Q)(int16_t)(uint16_t)((uint16_t)v2 - (uint16_t)v1);
+}
 // machine-integer differences wrap; the conversion to Q rounds to nearest
 template <class Q> __device__ __forceinline__ Q tdiff(int32_t v2, int32_t v1) {
     return (Q)(int32_t)((uint32_t)v2 - (uint32_t)v1);
@@ -322,6 +334,15 @@ __device__ __forceinline__ bool fast_f32_pos(float mu, float p1h, float p1l, flo
 }
 
 template <class T> __device__ __forceinline__ T shfl_down1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+template <> __device__ __forceinline__ int8_t shfl_down1<int8_t>(int8_t v) {
+    return (int8_t)__shfl_down_sync(0xffffffffu, (int)v, 1);
+}
+template <> __device__ __forceinline__ uint8_t shfl_down1<uint8_t>(uint8_t v) {
+    return (uint8_t)__shfl_down_sync(0xffffffffu, (unsigned)v, 1);
+}
+template <> __device__ __forceinline__ int16_t shfl_down1<int16_t>(int16_t v) {
+    return (int16_t)__shfl_down_sync(0xffffffffu, (int)v, 1);
+}
 template <> __device__ __forceinline__ h16 shfl_down1<h16>(h16 v) {
     h16 r;
     r.b = (uint16_t)__shfl_down_sync(0xffffffffu, (unsigned)v.b, 1);

@@ -171,6 +171,22 @@ template <> __device__ __forceinline__ void store8<int64_t>(int64_t *dst, const 
 #pragma unroll
     for (int k = 0; k < 4; k++) d[k] = make_longlong2(v[2 * k], v[2 * k + 1]);
 }
+template <> __device__ __forceinline__ void store8<int16_t>(int16_t *dst, const int16_t (&v)[8]) {
+    uint4 q;
+    q.x = (uint16_t)v[0] | (uint32_t)(uint16_t)v[1] << 16;
+    q.y = (uint16_t)v[2] | (uint32_t)(uint16_t)v[3] << 16;
+    q.z = (uint16_t)v[4] | (uint32_t)(uint16_t)v[5] << 16;
+    q.w = (uint16_t)v[6] | (uint32_t)(uint16_t)v[7] << 16;
+    *reinterpret_cast<uint4 *>(dst) = q;
+}
+template <class T> __device__ __forceinline__ void store8_bytes(T *dst, const T (&v)[8]) {
+    uint2 q;
+    q.x = (uint8_t)v[0] | (uint32_t)(uint8_t)v[1] << 8 | (uint32_t)(uint8_t)v[2] << 16 | (uint32_t)(uint8_t)v[3] << 24;
+    q.y = (uint8_t)v[4] | (uint32_t)(uint8_t)v[5] << 8 | (uint32_t)(uint8_t)v[6] << 16 | (uint32_t)(uint8_t)v[7] << 24;
+    *reinterpret_cast<uint2 *>(dst) = q;
+}
+template <> __device__ __forceinline__ void store8<int8_t>(int8_t *dst, const int8_t (&v)[8]) { store8_bytes(dst, v); }
+template <> __device__ __forceinline__ void store8<uint8_t>(uint8_t *dst, const uint8_t (&v)[8]) { store8_bytes(dst, v); }
 template <> __device__ __forceinline__ void store8<h16>(h16 *dst, const h16 (&v)[8]) {
     uint4 q;
     q.x = v[0].b | (uint32_t)v[1].b << 16;
@@ -180,6 +196,25 @@ template <> __device__ __forceinline__ void store8<h16>(h16 *dst, const h16 (&v)
     *reinterpret_cast<uint4 *>(dst) = q;
 }
 template <class T> __device__ __forceinline__ void load8(const T *src, T (&v)[8]);
+template <> __device__ __forceinline__ void load8<int16_t>(const int16_t *src, int16_t (&v)[8]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(src);
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[2 * k] = (int16_t)(uint16_t)(w[k] & 0xffffu);
+        v[2 * k + 1] = (int16_t)(uint16_t)(w[k] >> 16);
+    }
+}
+template <class T> __device__ __forceinline__ void load8_bytes(const T *src, T (&v)[8]) {
+    const uint2 q = *reinterpret_cast<const uint2 *>(src);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[k] = (T)(uint8_t)(q.x >> (8 * k));
+        v[4 + k] = (T)(uint8_t)(q.y >> (8 * k));
+    }
+}
+template <> __device__ __forceinline__ void load8<int8_t>(const int8_t *src, int8_t (&v)[8]) { load8_bytes(src, v); }
+template <> __device__ __forceinline__ void load8<uint8_t>(const uint8_t *src, uint8_t (&v)[8]) { load8_bytes(src, v); }
 template <> __device__ __forceinline__ void load8<h16>(const h16 *src, h16 (&v)[8]) {
     const uint4 q = *reinterpret_cast<const uint4 *>(src);
     const uint32_t w[4] = {q.x, q.y, q.z, q.w};

@@ -4,10 +4,11 @@
 Drop-in GPU back end for Meshing.jl.  Loading this module adds methods of
 `Meshing.isosurface` that are more specific than the reference's
 (src/marching_cubes.jl:27, src/marching_tetrahedra.jl:129): dense
-`Array{T,3}` volumes with `T ∈ {UInt16, Int32, Int64, Float16, Float32, Float64}` and
+`Array{T,3}` volumes with `T ∈ {UInt8, Int8, Int16, UInt16, Int32, Int64, Float16, Float32,
+Float64}` and
 iso / eps / range endpoints of type Float32, Float64 or Int64 run on the GPU through
 `libmeshing_gb300.so` (Float16 data with a Float32 or Float64 iso).  Every other
-combination (Float16 data with an Int iso, Int8/Int16 data, ForwardDiff.Dual,
+combination (Float16 data with an Int iso, other machine integers, ForwardDiff.Dual,
 mixed endpoint types) reaches the reference method through `invoke`, i.e.
 ordinary dispatch, not a fallback inside the library.
 Results are identical to the reference's: the same element types, vertex
@@ -45,7 +46,7 @@ struct MeshParams
     range::NTuple{6,Float64}
 end
 
-const DevEl = Union{UInt16,Int32,Int64,Float16,Float32,Float64}
+const DevEl = Union{UInt8,Int8,Int16,UInt16,Int32,Int64,Float16,Float32,Float64}
 const DevScalar = Union{Float32,Float64,Int64}
 
 dtcode(::Type{UInt16}) = Int32(1)
@@ -54,6 +55,9 @@ dtcode(::Type{Float64}) = Int32(3)
 dtcode(::Type{Int64}) = Int32(4)
 dtcode(::Type{Int32}) = Int32(5)
 dtcode(::Type{Float16}) = Int32(6)
+dtcode(::Type{Int16}) = Int32(7)
+dtcode(::Type{Int8}) = Int32(8)
+dtcode(::Type{UInt8}) = Int32(9)
 # promote(Int, Float16) is Float16: that quotient runs in Float16 arithmetic, left to the reference
 device_ok(::Type{T}, ::Type{I}) where {T,I} = !(T === Float16 && I === Int64)
 dtcode(::Type) = Int32(0)

@@ -37,7 +37,7 @@
 
 #include "ref_luts.h"
 
-enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4, ORC_I32 = 5, ORC_F16 = 6 };
+enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4, ORC_I32 = 5, ORC_F16 = 6, ORC_I16 = 7, ORC_I8 = 8, ORC_U8 = 9 };
 enum { ORC_MC = 0, ORC_MT = 1, ORC_NSN = 2 };
 enum { ORC_OK = 0, ORC_EINVAL = 1, ORC_ENOMEM = 2 };
 
@@ -82,7 +82,8 @@ static int out_type(const int *tys, int n) {
     return ORC_F64; /* float(Integer) == Float64 */
 }
 
-static int is_wide_int(int ty) { return ty == ORC_I32 || ty == ORC_I64; }
+/* signed machine integers: values travel as Int64 bit patterns in the double slots */
+static int is_wide_int(int ty) { return ty == ORC_I32 || ty == ORC_I64 || ty == ORC_I16 || ty == ORC_I8; }
 static double pun(int64_t i) {
     double d;
     memcpy(&d, &i, sizeof d);
@@ -110,6 +111,9 @@ static double load(const orc_ctx *c, int64_t x, int64_t y, int64_t z) {
     int64_t i = x + c->nx * (y + c->ny * z);
     switch (c->T) {
     case ORC_U16: return (double)((const uint16_t *)c->vol)[i];
+    case ORC_U8: return (double)((const uint8_t *)c->vol)[i];
+    case ORC_I16: return pun((int64_t)((const int16_t *)c->vol)[i]);
+    case ORC_I8: return pun((int64_t)((const int8_t *)c->vol)[i]);
     case ORC_F16: return half_value(((const uint16_t *)c->vol)[i]);
     case ORC_F32: return (double)((const float *)c->vol)[i];
     case ORC_I32: return pun((int64_t)((const int32_t *)c->vol)[i]);
@@ -138,8 +142,10 @@ static double quotient(const orc_ctx *c, double v1, double v2) {
     if (is_wide_int(c->T)) {
         const int64_t a = unpun(v1), b = unpun(v2);
         /* v2 - v1 in the data type, wrapping */
-        const int64_t d = c->T == ORC_I32 ? (int64_t)(int32_t)((uint32_t)b - (uint32_t)a)
-                                          : (int64_t)((uint64_t)b - (uint64_t)a);
+        const int64_t d = c->T == ORC_I32   ? (int64_t)(int32_t)((uint32_t)b - (uint32_t)a)
+                          : c->T == ORC_I16 ? (int64_t)(int16_t)(uint16_t)((uint16_t)b - (uint16_t)a)
+                          : c->T == ORC_I8  ? (int64_t)(int8_t)(uint8_t)((uint8_t)b - (uint8_t)a)
+                                            : (int64_t)((uint64_t)b - (uint64_t)a);
         if (c->Q == ORC_F32) {  /* Float32 iso: Float32(iso) - Float32(v1), Float32(v2 - v1) */
             const double num = rnd(ORC_F32, (double)(float)c->isoq - (double)(float)a);
             return rnd(ORC_F32, num / (double)(float)d);
@@ -153,6 +159,8 @@ static double quotient(const orc_ctx *c, double v1, double v2) {
     }
     if (c->T == ORC_U16)
         den = (double)(uint16_t)((uint16_t)v2 - (uint16_t)v1); /* UInt16 wraps */
+    else if (c->T == ORC_U8)
+        den = (double)(uint8_t)((uint8_t)v2 - (uint8_t)v1); /* UInt8 wraps */
     else if (c->T == ORC_F32)
         den = rnd(ORC_F32, v2 - v1);
     else if (c->T == ORC_F16)
@@ -476,7 +484,9 @@ static int run_nsn(const orc_ctx *c, orc_mesh *m) {
 static int setup(orc_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int alg, int I, double iso,
                  int E, double eps, int R, const double *rg) {
     memset(c, 0, sizeof(*c));
-    if (T != ORC_U16 && T != ORC_F32 && T != ORC_F64 && T != ORC_I32 && T != ORC_I64 && T != ORC_F16) return ORC_EINVAL;
+    if (T != ORC_U16 && T != ORC_F32 && T != ORC_F64 && T != ORC_I32 && T != ORC_I64 && T != ORC_F16 && T != ORC_I16 &&
+        T != ORC_I8 && T != ORC_U8)
+        return ORC_EINVAL;
     if (T == ORC_F16 && I == ORC_I64) return ORC_EINVAL; /* promote(Int, Float16): Float16 arithmetic, not restated */
     if (I != ORC_F32 && I != ORC_F64 && I != ORC_I64) return ORC_EINVAL;
     if (R != ORC_F32 && R != ORC_F64 && R != ORC_I64) return ORC_EINVAL;

@@ -50,10 +50,16 @@ def _promote(*tys):
         return np.int64
     if np.int32 in tys:
         return np.int32
-    return np.uint16
+    if np.int16 in tys:
+        return np.int16
+    if np.int8 in tys:
+        return np.int8
+    if np.uint16 in tys:
+        return np.uint16
+    return np.uint8
 
 
-_INTS = (np.uint16, np.int32, np.int64)
+_INTS = (np.uint16, np.int32, np.int64, np.int16, np.int8, np.uint8)
 
 
 def _float(t):

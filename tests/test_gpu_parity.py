@@ -223,7 +223,7 @@ def test_fill_without_count_is_rejected(pkg, cuda):
 
 
 @pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
-@pytest.mark.parametrize('dt', [np.int32, np.int64])
+@pytest.mark.parametrize('dt', [np.int32, np.int64, np.int16, np.int8, np.uint8])
 def test_integer_volumes(pkg, oracle, cuda, alg, dt):
     # test/runtests.jl:66-75 runs every algorithm on rand(Int, 10, 10, 10): exact
     # integer-vs-iso comparison, v2 - v1 wrapping in the data type, the quotient in

@@ -152,7 +152,7 @@ def test_uint16_wraparound_is_reproduced(oracle):
     assert np.isclose(v[0, 0], -1 + mu * 2)  # edge 1 runs along +x from x=-1
 
 
-@pytest.mark.parametrize('dt', [np.int32, np.int64])
+@pytest.mark.parametrize('dt', [np.int32, np.int64, np.int16, np.int8, np.uint8])
 def test_integer_volumes_c_matches_python(oracle, dt):
     # Int32 / Int64 volumes (test/runtests.jl:66-75 runs every algorithm on rand(Int, ...)):
     # exact integer-vs-iso comparison, v2 - v1 wrapping in the data type, and the
