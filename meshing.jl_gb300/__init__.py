@@ -18,7 +18,8 @@ from .api import (MarchingCubes, MarchingTetrahedra, NaiveSurfaceNets, AbstractM
                   isosurface_device, output_float_bits, make_params, default_context)
 from .batch import Batch
 from .serve import Server
+from . import ingest
 
 __all__ = ['isosurface', 'isosurface_device', 'MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets',
            'AbstractMeshingAlgorithm', 'MeshError', 'Context', 'MeshParams', 'output_float_bits', 'make_params',
-           'default_context', 'load_library', 'Batch', 'Server']
+           'default_context', 'load_library', 'Batch', 'Server', 'ingest']
