@@ -89,6 +89,13 @@ MESH_API int mesh_ctx_create(int device, mesh_ctx **out);
 MESH_API void mesh_ctx_destroy(mesh_ctx *ctx);
 /* Makes the context issue its work on `stream` (a cudaStream_t; NULL = the context's own). */
 MESH_API int mesh_ctx_set_stream(mesh_ctx *ctx, void *stream);
+/* No counterpart in the reference.  Until reset with (0, 0), the volumes of the
+ * context's calls are x samples x_first .. x_first+nx-1 of a volume whose x axis
+ * has nx_total samples: node coordinates are those of LinRange(first(X),
+ * last(X), nx_total), so a Marching Cubes x slab meshes exactly as that part of
+ * the whole volume (x is the outermost emission axis: slab meshes concatenate
+ * into the whole one, face indices offset by the vertices before them). */
+MESH_API int mesh_set_x_window(mesh_ctx *ctx, int64_t x_first, int64_t nx_total);
 MESH_API const char *mesh_status_string(int status);
 /* Last error message recorded on `ctx` (empty string if none). */
 MESH_API const char *mesh_ctx_last_error(const mesh_ctx *ctx);

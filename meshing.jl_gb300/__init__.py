@@ -15,11 +15,11 @@ on the GPU through the C ABI (include/meshing_gb300.h); there is no CPU path.
 """
 from ._lib import Context, MeshError, MeshParams, load as load_library
 from .api import (MarchingCubes, MarchingTetrahedra, NaiveSurfaceNets, AbstractMeshingAlgorithm, isosurface,
-                  isosurface_device, output_float_bits, make_params, default_context)
+                  isosurface_device, isosurface_slabs, output_float_bits, make_params, default_context)
 from .batch import Batch
 from .serve import Server
 from . import ingest
 
-__all__ = ['isosurface', 'isosurface_device', 'MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets',
+__all__ = ['isosurface', 'isosurface_device', 'isosurface_slabs', 'MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets',
            'AbstractMeshingAlgorithm', 'MeshError', 'Context', 'MeshParams', 'output_float_bits', 'make_params',
            'default_context', 'load_library', 'Batch', 'Server', 'ingest']

@@ -16,7 +16,8 @@ STATUS = {0: 'MESH_OK', 1: 'MESH_EINVAL', 2: 'MESH_ENOMEM', 3: 'MESH_ECUDA', 4: 
           6: 'MESH_ECAPACITY', 7: 'MESH_ETOOLARGE', 8: 'MESH_ESCRATCH', 9: 'MESH_EBUDGET', 10: 'MESH_EBUSY'}
 
 # every symbol the header declares
-EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_ctx_set_stream', 'mesh_status_string',
+EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_ctx_set_stream', 'mesh_set_x_window',
+           'mesh_status_string',
            'mesh_ctx_last_error', 'mesh_output_float_bits', 'mesh_count', 'mesh_fill', 'mesh_extract_device',
            'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times', 'mesh_extract_noalloc',
            'mesh_batch_create', 'mesh_batch_destroy', 'mesh_batch_count', 'mesh_batch_run', 'mesh_batch_sync',
@@ -56,6 +57,7 @@ def load():
         'mesh_ctx_create': (c_int, [c_int, P(vp)]),
         'mesh_ctx_destroy': (None, [vp]),
         'mesh_ctx_set_stream': (c_int, [vp, vp]),
+        'mesh_set_x_window': (c_int, [vp, ctypes.c_int64, ctypes.c_int64]),
         'mesh_status_string': (ctypes.c_char_p, [c_int]),
         'mesh_ctx_last_error': (ctypes.c_char_p, [vp]),
         'mesh_output_float_bits': (c_int, [c_int, P(MeshParams), P(c_int)]),

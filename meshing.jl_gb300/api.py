@@ -221,6 +221,62 @@ def isosurface(A, *args, ctx=None):
     return verts, faces
 
 
+def isosurface_slabs(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), slab_cells=None, slab_bytes=4 << 30,
+                     ctx=None):
+    """Marching Cubes of a host volume larger than device memory, one x slab at a time.
+
+    x is the outermost axis of the reference's emission order
+    (src/marching_cubes.jl:40), so the meshes of consecutive x slabs of cells,
+    concatenated with face indices offset by the vertices before them, are the
+    mesh of the whole volume.  Slab k holds cells [c0, c1) and samples
+    [c0, c1]; its node coordinates are those of the whole volume's LinRange
+    (mesh_set_x_window).  ``A`` is a numpy array (or memmap) indexed [x, y, z];
+    ``slab_cells`` cells per slab, or as many as fit ``slab_bytes`` of volume.
+    Returns numpy (points, faces) equal to ``isosurface(A, method, X, Y, Z)``.
+    MarchingTetrahedra and NaiveSurfaceNets share vertices between cells on
+    both sides of a slab boundary, so they are not split.
+    """
+    method = method or MarchingCubes()
+    if not isinstance(method, MarchingCubes):
+        raise TypeError('only MarchingCubes meshes split into x slabs')
+    p = make_params(method, X, Y, Z)
+    dt = _VOL_DT.get(np.dtype(A.dtype))
+    if dt is None or A.ndim != 3:
+        raise TypeError('3-D volume of a supported eltype expected')
+    nx, ny, nz = A.shape
+    lib = _lib.load()
+    bits = ctypes.c_int()
+    check(lib.mesh_output_float_bits(dt, ctypes.byref(p), ctypes.byref(bits)))
+    ft = np.float32 if bits.value == 32 else np.float64
+    if slab_cells is None:
+        plane = ny * nz * A.dtype.itemsize
+        slab_cells = max(1, int(slab_bytes // max(plane, 1)) - 1)
+    c = ctx or default_context(0)
+    c.set_stream(None)
+    vs, fs, voff = [], [], 0
+    try:
+        for c0 in range(0, max(nx - 1, 0), slab_cells):
+            c1 = min(c0 + slab_cells, nx - 1)
+            S = np.asfortranarray(A[c0:c1 + 1])
+            check(lib.mesh_set_x_window(c.handle, c0, nx), c.handle)
+            nv, nf = ctypes.c_int64(), ctypes.c_int64()
+            check(lib.mesh_count(c.handle, ctypes.c_void_p(S.ctypes.data), dt, S.shape[0], ny, nz, 0,
+                                 ctypes.byref(p), ctypes.byref(nv), ctypes.byref(nf)), c.handle)
+            v = np.empty((nv.value, 3), dtype=ft)
+            f = np.empty((nf.value, 3), dtype=np.int64)
+            check(lib.mesh_fill(c.handle, ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(f.ctypes.data), 0),
+                  c.handle)
+            f += voff
+            voff += nv.value
+            vs.append(v)
+            fs.append(f)
+    finally:
+        lib.mesh_set_x_window(c.handle, 0, 0)
+    if not vs:
+        return np.empty((0, 3), dtype=ft), np.empty((0, 3), dtype=np.int64)
+    return np.concatenate(vs), np.concatenate(fs)
+
+
 def isosurface_device(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), verts=None, faces=None, counts=None,
                       ctx=None):
     """Device-resident extraction with no host round trip (mesh_extract_device).

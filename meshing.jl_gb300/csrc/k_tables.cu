@@ -17,13 +17,16 @@ namespace {
 // LinRange node coordinates, spacings and their float forms, computed on the
 // device with the host path's arithmetic: L((1 - t)*a + t*b), t = i/(n-1), every
 // operation rounded separately.
-// Entry k of the table block at `tabs` for nx, ny, nz nodes.
+// Entry k of the table block at `tabs` for nx, ny, nz nodes.  The x nodes are
+// nodes xoff .. xoff+nx-1 of an x axis of nxt nodes (a slab of a larger volume;
+// xoff = 0, nxt = nx for a whole volume).
 __device__ __forceinline__ void table_entry(double *tabs, int64_t k, int64_t nx, int64_t ny, int64_t nz, double x0,
-                                            double x1, double y0, double y1, double z0, double z1, int L32) {
+                                            double x1, double y0, double y1, double z0, double z1, int L32,
+                                            int64_t xoff = 0, int64_t nxt = 0) {
     const int64_t ntab = nx + ny + nz;
     double *hp = tabs, *hd = tabs + ntab;
     float *hpf = (float *)(tabs + 2 * ntab), *hdf = hpf + ntab, *hs = hdf + ntab;
-    int64_t i = k, n = nx;
+    int64_t i = k + xoff, n = nxt > 0 ? nxt : nx;
     double a = x0, b = x1;
     if (k >= nx + ny) {
         i = k - nx - ny; n = nz; a = z0; b = z1;
@@ -57,10 +60,10 @@ __device__ __forceinline__ void table_entry(double *tabs, int64_t k, int64_t nx,
 }
 
 __global__ void k_tables(double *tabs, int64_t nx, int64_t ny, int64_t nz, double x0, double x1, double y0,
-                         double y1, double z0, double z1, int L32) {
+                         double y1, double z0, double z1, int L32, int64_t xoff, int64_t nxt) {
     const int64_t ntab = nx + ny + nz;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ntab; k += (int64_t)gridDim.x * blockDim.x)
-        table_entry(tabs, k, nx, ny, nz, x0, x1, y0, y1, z0, z1, L32);
+        table_entry(tabs, k, nx, ny, nz, x0, x1, y0, y1, z0, z1, L32, xoff, nxt);
 }
 
 __global__ void k_tables_batch(const TabJob *jobs, int L32) {
@@ -83,10 +86,10 @@ cudaError_t launch_tables_batch(const TabJob *jobs, int njobs, int64_t max_ntab,
 }
 
 cudaError_t launch_tables(double *tabs, int64_t nx, int64_t ny, int64_t nz, const double *range, int L32,
-                          cudaStream_t s) {
+                          cudaStream_t s, int64_t xoff, int64_t nxt) {
     const int64_t ntab = nx + ny + nz;
     k_tables<<<(int)std::min<int64_t>((ntab + 255) / 256, 1024), 256, 0, s>>>(
-        tabs, nx, ny, nz, range[0], range[1], range[2], range[3], range[4], range[5], L32);
+        tabs, nx, ny, nz, range[0], range[1], range[2], range[3], range[4], range[5], L32, xoff, nxt);
     return cudaGetLastError();
 }
 

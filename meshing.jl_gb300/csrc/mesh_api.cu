@@ -229,7 +229,9 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     // hi/lo float split of the nodes and spacings, computed on the device
     const int64_t ntab = nx + ny + nz;
     if ((e = c->tabs.ensure(table_bytes(ntab))) != cudaSuccess) return cuda_fail(c, e, "table buffer");
-    if ((e = launch_tables((double *)c->tabs.ptr, nx, ny, nz, p->range, L32, c->stream)) != cudaSuccess)
+    if (c->win_nx && c->win_x0 + nx > c->win_nx) return fail(c, MESH_EINVAL, "volume extends past its x window");
+    if ((e = launch_tables((double *)c->tabs.ptr, nx, ny, nz, p->range, L32, c->stream, c->win_x0, c->win_nx)) !=
+        cudaSuccess)
         return cuda_fail(c, e, "table launch");
     bind_tables(P, (double *)c->tabs.ptr, nx, ny, nz);
     P.force_fp64 = c->force_fp64;
@@ -499,6 +501,16 @@ void mesh_ctx_destroy(mesh_ctx *c) {
 int mesh_ctx_set_stream(mesh_ctx *c, void *stream) {
     if (!c) return MESH_EINVAL;
     c->stream = stream ? (cudaStream_t)stream : c->own;
+    return MESH_OK;
+}
+
+int mesh_set_x_window(mesh_ctx *c, int64_t x_first, int64_t nx_total) {
+    if (!c) return MESH_EINVAL;
+    if (x_first < 0 || nx_total < 0 || (nx_total == 0 && x_first != 0) || nx_total > ((int64_t)1 << POS_BITS))
+        return fail(c, MESH_EINVAL, "invalid x window");
+    c->win_x0 = x_first;
+    c->win_nx = nx_total;
+    c->have_plan = 0;
     return MESH_OK;
 }
 

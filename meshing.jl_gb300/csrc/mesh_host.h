@@ -57,6 +57,9 @@ struct mesh_ctx {
     int Q64 = 0, A64 = 0, P64 = 0;
     int64_t nverts = 0, nfaces = 0, nactive = 0;
     int64_t ent_cap_seen = 0;  // largest active-cell list prepared on this context
+    // mesh_set_x_window: the volumes of the following calls are x nodes
+    // win_x0 .. win_x0+nx-1 of an x axis of win_nx nodes (win_nx == 0: whole axis)
+    int64_t win_x0 = 0, win_nx = 0;
     std::string msg;
     // stage timing (diagnostics)
     int timing = 0;

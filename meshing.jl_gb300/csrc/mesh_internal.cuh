@@ -187,8 +187,9 @@ inline void bind_tables(Plan &P, const double *dp, int64_t nx, int64_t ny, int64
 }
 
 // Launchers (each returns cudaError_t of the launch).
+// xoff / nxt: the volume is x nodes xoff .. xoff+nx-1 of an axis of nxt nodes (0, 0: the whole axis).
 cudaError_t launch_tables(double *tabs, int64_t nx, int64_t ny, int64_t nz, const double *range, int L32,
-                          cudaStream_t s);
+                          cudaStream_t s, int64_t xoff = 0, int64_t nxt = 0);
 // Tables of many volumes: job i fills the block at dst[i] (one CTA row per job).
 struct TabJob {
     double *dst;

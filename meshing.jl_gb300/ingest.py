@@ -187,8 +187,9 @@ def to_device(zyx, device='cuda'):
     """A [z][y][x] C-order numpy array as a CUDA tensor indexed [x, y, z] (Julia
     layout), copied from pinned host memory."""
     import torch
-    zyx = np.ascontiguousarray(zyx)
-    host = torch.from_numpy(zyx).pin_memory()
+    tdt = torch.from_numpy(np.empty(0, dtype=zyx.dtype)).dtype
+    host = torch.empty(zyx.shape, dtype=tdt, pin_memory=True)
+    host.numpy()[...] = zyx  # one copy, straight into pinned memory
     dev = host.to(device, non_blocking=True)
     torch.cuda.current_stream(dev.device).synchronize()
     return dev.permute(2, 1, 0)
