@@ -129,6 +129,19 @@ MESH_API int mesh_extract_device(mesh_ctx *ctx, const void *vol, int vol_dtype, 
 /* Waits for the context's outstanding work and reports device-side errors. */
 MESH_API int mesh_ctx_sync(mesh_ctx *ctx);
 
+/* No counterpart in Meshing.jl (post-processing of a finished mesh, the
+ * published area-weighted rule of GeometryBasics' normals(vertices, faces)):
+ * normal i = normalize(sum over the faces f using vertex i of
+ * cross(v[f2] - v[f1], v[f3] - v[f1])), accumulated in Float64 and written in
+ * the vertex type; a vertex on no face of non-zero area gets (0, 0, 0).
+ * `verts` (nverts x 3, float_bits 32 or 64), `faces` (nfaces x 3, 1-based) and
+ * `normals` (nverts x 3, the vertex type) are device pointers.  Asynchronous on
+ * the context stream; mesh_ctx_sync() reports MESH_EDEVICE if a face index
+ * lies outside 1..nverts (that face is skipped).  Uses the context's error word:
+ * a two-phase call in progress must finish (mesh_fill) first. */
+MESH_API int mesh_vertex_normals(mesh_ctx *ctx, const void *verts, int float_bits, int64_t nverts,
+                                 const int64_t *faces, int64_t nfaces, void *normals);
+
 /* Diagnostics (no counterpart in the reference, which has no instrumentation):
  * with timing enabled the context brackets every kernel launch with CUDA
  * events on its stream.  mesh_ctx_stage_times waits for them and returns, per

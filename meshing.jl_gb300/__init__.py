@@ -18,8 +18,8 @@ from .api import (MarchingCubes, MarchingTetrahedra, NaiveSurfaceNets, AbstractM
                   isosurface_device, isosurface_slabs, output_float_bits, make_params, default_context)
 from .batch import Batch
 from .serve import Server
-from . import ingest
+from . import export, ingest
 
 __all__ = ['isosurface', 'isosurface_device', 'isosurface_slabs', 'MarchingCubes', 'MarchingTetrahedra', 'NaiveSurfaceNets',
            'AbstractMeshingAlgorithm', 'MeshError', 'Context', 'MeshParams', 'output_float_bits', 'make_params',
-           'default_context', 'load_library', 'Batch', 'Server', 'ingest']
+           'default_context', 'load_library', 'Batch', 'Server', 'export', 'ingest']

@@ -20,6 +20,7 @@ EXPORTS = ('mesh_params_default', 'mesh_ctx_create', 'mesh_ctx_destroy', 'mesh_c
            'mesh_status_string',
            'mesh_ctx_last_error', 'mesh_output_float_bits', 'mesh_count', 'mesh_fill', 'mesh_extract_device',
            'mesh_ctx_sync', 'mesh_ctx_enable_timing', 'mesh_ctx_stage_times', 'mesh_extract_noalloc',
+           'mesh_vertex_normals',
            'mesh_batch_create', 'mesh_batch_destroy', 'mesh_batch_count', 'mesh_batch_run', 'mesh_batch_sync',
            'mesh_batch_outputs', 'mesh_batch_set_graph', 'mesh_batch_set_knobs', 'mesh_batch_knobs', 'mesh_batch_tune',
            'mesh_server_create', 'mesh_server_destroy', 'mesh_server_last_error', 'mesh_server_submit',
@@ -58,6 +59,7 @@ def load():
         'mesh_ctx_destroy': (None, [vp]),
         'mesh_ctx_set_stream': (c_int, [vp, vp]),
         'mesh_set_x_window': (c_int, [vp, ctypes.c_int64, ctypes.c_int64]),
+        'mesh_vertex_normals': (c_int, [vp, vp, c_int, ctypes.c_int64, vp, ctypes.c_int64, vp]),
         'mesh_status_string': (ctypes.c_char_p, [c_int]),
         'mesh_ctx_last_error': (ctypes.c_char_p, [vp]),
         'mesh_output_float_bits': (c_int, [c_int, P(MeshParams), P(c_int)]),

@@ -488,7 +488,8 @@ void mesh_ctx_destroy(mesh_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->vol, &c->tabs, &c->cnt, &c->base, &c->flags, &c->scan, &c->misc, &c->out_v, &c->out_f, &c->ent};
+    DevBuf *bufs[] = {&c->vol,   &c->tabs,  &c->cnt,   &c->base, &c->flags, &c->scan,
+                      &c->misc,  &c->out_v, &c->out_f, &c->ent,  &c->nrm};
     for (DevBuf *b : bufs) b->release();
     for (auto &v : c->ev_pairs)
         for (cudaEvent_t e : v) cudaEventDestroy(e);

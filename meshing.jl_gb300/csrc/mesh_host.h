@@ -51,6 +51,7 @@ struct mesh_ctx {
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     mesh::DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f, ent;
+    mesh::DevBuf nrm;  // mesh_vertex_normals: double accumulators
     int64_t *h_misc = nullptr;  // pinned: totals[NCNT], err
     mesh::Plan plan{};
     int have_plan = 0;
