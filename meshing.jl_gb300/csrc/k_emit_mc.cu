@@ -28,7 +28,7 @@ namespace mesh {
 
 namespace {
 
-constexpr int U = 4;     // z planes loaded ahead (only active chunks are walked)
+constexpr int U = 8;     // z planes loaded ahead (only active chunks are walked)
 // A chunk's last loaded plane becomes the next chunk's first (lov = v[U-1]), so a
 // group of U planes must never straddle a chunk boundary.
 static_assert(ZC % U == 0, "U must divide the activity chunk");
@@ -50,30 +50,30 @@ struct CompactSmem {
 // per cell row, one lookup of the case's packed word (mesh_case.cuh); the
 // lanes whose cell is active write its entry at the piece's entry offset plus
 // the entries before it in the chunk (bits 23.. of the running word).
-template <class T>
+template <class T, int NR>
 __device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int w, int lane, int tx, int ty, int seg,
                                              uint32_t vol) {
     const T *volp = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
     const int64_t np = p.pstride;
     const int xs = tx * TILE_X + lane;
-    const int y0 = ty * WY;
+    const int y0 = ty * NR;
     const int zbeg = seg * p.zs;
     const int zend = min(zbeg + p.zs, p.cz);
     const bool cellx = lane < TILE_X && xs < p.cx;
 
-    bool rowok[WY + 1];
-    const T *rowp[WY + 1];
+    bool rowok[NR + 1];
+    const T *rowp[NR + 1];
 #pragma unroll
-    for (int r = 0; r <= WY; r++) {
+    for (int r = 0; r <= NR; r++) {
         rowok[r] = xs < p.nx && y0 + r < p.ny;
         rowp[r] = rowok[r] ? volp + xs + p.nx * (int64_t)(y0 + r) : volp;
     }
     const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
-    uint32_t rmask[WY];
-    int64_t ba[WY];  // entry offset of each row's piece
+    uint32_t rmask[NR];
+    int64_t ba[NR];  // entry offset of each row's piece
 #pragma unroll
-    for (int r = 0; r < WY; r++) {
+    for (int r = 0; r < NR; r++) {
         rmask[r] = (cellx && y0 + r < p.cy) ? 0xffffffffu : 0u;
         ba[r] = 0;
         long long v0 = 0, f0 = 0;
@@ -97,14 +97,14 @@ __device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int
         if (k < nch) {
             const uint8_t *fp = p.flags + ((chunk0 + k) * p.tiles_x + tx) * p.cy + y0;
 #pragma unroll
-            for (int r = 0; r < WY; r++)
+            for (int r = 0; r < NR; r++)
                 if (y0 + r < p.cy) any |= fp[r];
         }
         return __ballot_sync(FULL, any != 0u);
     };
 
-    uint32_t mlo[WY + 1];
-    T lov[WY + 1];  // samples of plane `have`
+    uint32_t mlo[NR + 1];
+    T lov[NR + 1];  // samples of plane `have`
     int have = -1;
     for (int g = 0; 32 * g < nch; g++) {
         uint32_t todo = active(g);
@@ -115,30 +115,30 @@ __device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int
             const int zc1 = min(zc0 + ZC, zend);
             if (have != zc0) {
 #pragma unroll
-                for (int r = 0; r <= WY; r++) {
+                for (int r = 0; r <= NR; r++) {
                     lov[r] = rowok[r] ? ldv(rowp[r] + sxy * (int64_t)zc0) : T(0);
                     mlo[r] = __ballot_sync(FULL, rowok[r] && below(lov[r], p));
                 }
             }
-            uint32_t pk[WY];
+            uint32_t pk[NR];
 #pragma unroll
-            for (int r = 0; r < WY; r++) pk[r] = 0;
+            for (int r = 0; r < NR; r++) pk[r] = 0;
             for (int z = zc0; z < zc1; z += U) {
-                T v[U][WY + 1];
+                T v[U][NR + 1];
                 const int64_t off = sxy * (int64_t)(z + 1);
 #pragma unroll
                 for (int u = 0; u < U; u++)
 #pragma unroll
-                    for (int r = 0; r <= WY; r++)
+                    for (int r = 0; r <= NR; r++)
                         v[u][r] = (rowok[r] && z + 1 + u <= zc1) ? ldv(rowp[r] + off + sxy * u) : T(0);
 #pragma unroll
                 for (int u = 0; u < U; u++) {
                     const int zc = z + u;
                     if (zc >= zc1) break;  // warp-uniform
-                    uint32_t mhi[WY + 1];
+                    uint32_t mhi[NR + 1];
                     uint32_t all1 = xval, any1 = 0;
 #pragma unroll
-                    for (int r = 0; r <= WY; r++) {
+                    for (int r = 0; r <= NR; r++) {
                         mhi[r] = __ballot_sync(FULL, rowok[r] && below(v[u][r], p));
                         all1 &= mlo[r] & mhi[r];
                         any1 |= mlo[r] | mhi[r];
@@ -151,7 +151,7 @@ __device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int
                         T l1 = shfl_down1(l0), h1 = shfl_down1(h0);
                         uint32_t n0 = row_field(mlo[0], mhi[0], lane);
 #pragma unroll
-                        for (int r = 0; r < WY; r++) {
+                        for (int r = 0; r < NR; r++) {
                             const T L0 = u == 0 ? lov[r + 1] : v[u == 0 ? 0 : u - 1][r + 1];
                             const T H0 = v[u][r + 1];
                             const T L1 = shfl_down1(L0), H1 = shfl_down1(H0);
@@ -187,16 +187,16 @@ __device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int
                         }
                     }
 #pragma unroll
-                    for (int r = 0; r <= WY; r++) mlo[r] = mhi[r];
+                    for (int r = 0; r <= NR; r++) mlo[r] = mhi[r];
                 }
 #pragma unroll
-                for (int r = 0; r <= WY; r++) lov[r] = v[U - 1][r];
+                for (int r = 0; r <= NR; r++) lov[r] = v[U - 1][r];
             }
             // a chunk of ZC planes ends on whole groups of U (ZC % U == 0), so
             // lov / mlo hold plane zc1; after a shorter last chunk nothing follows
             have = zc1;
 #pragma unroll
-            for (int r = 0; r < WY; r++) {
+            for (int r = 0; r < NR; r++) {
                 ba[r] += pk[r] >> PK_A;
                 sm.bv[w][r][lane] += pk[r] & ((1u << PK_F) - 1u);
                 sm.bf[w][r][lane] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
@@ -206,44 +206,57 @@ __device__ __forceinline__ void compact_tile(const Plan &p, CompactSmem &sm, int
     __syncwarp();
 }
 
+// Cell rows per warp tile of the compaction.  One row (two sample rows per
+// plane) keeps the walk at 64 registers, 4 CTAs per SM, with 8 planes in flight
+// per warp; at 1024^3 Float32: 0.675 ms, against 0.73 with 4 planes, 0.79 with
+// 2 rows at 3 CTAs per SM and 1.00 with the classify tile's 4 rows at 2.
+constexpr int CR = 1;
+#ifndef COMPACT_MIN_CTAS
+#define COMPACT_MIN_CTAS 4
+#endif
+
 template <class T>
-__global__ void __launch_bounds__(256, 2) k_compact_mc(const Plan p, int nitems) {
+__global__ void __launch_bounds__(256, COMPACT_MIN_CTAS) k_compact_mc(const Plan p, int nitems) {
     __shared__ CompactSmem sm;
     load_tables_mc_packed(sm.pk, sm.cs);
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int tiles_y = (p.cy + CR - 1) / CR;
     // persistent warps: take (y tile, x tile, segment) items in order from a counter
     for (;;) {
         int item = 0;
         if (lane == 0) item = (int)atomicAdd(p.work, 1u);
         item = __shfl_sync(FULL, item, 0);
         if (item >= nitems) break;
-        const int ty = item % p.tiles_y;
-        const int tx = (item / p.tiles_y) % p.tiles_x;
-        const int seg = item / (p.tiles_y * p.tiles_x);
-        compact_tile<T>(p, sm, w, lane, tx, ty, seg, 0);
+        const int ty = item % tiles_y;
+        const int tx = (item / tiles_y) % p.tiles_x;
+        const int seg = item / (tiles_y * p.tiles_x);
+        compact_tile<T, CR>(p, sm, w, lane, tx, ty, seg, 0);
     }
 }
 
-// Batch: the work items of k_classify_batch, in the same order.
+// Batch: the work items of k_classify_batch, in the same order, each split
+// into its WY / CR tiles of CR cell rows.
 template <class T>
-__global__ void __launch_bounds__(256, 2) k_compact_batch(const Plan p) {
+__global__ void __launch_bounds__(256, COMPACT_MIN_CTAS) k_compact_batch(const Plan p) {
+    static_assert(WY % CR == 0, "compaction tiles split the classify tile");
+    constexpr int SUB = WY / CR;
     __shared__ CompactSmem sm;
     load_tables_mc_packed(sm.pk, sm.cs);
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (;;) {
-        unsigned item = 0;
+        unsigned item = 0;  // p.nitems * SUB < 2^31 (checked when the batch is planned)
         if (lane == 0) item = atomicAdd(p.work, 1u);
         item = __shfl_sync(FULL, item, 0);
-        if ((int64_t)item >= p.nitems) break;
-        const uint32_t v = p.item_vol[item];
+        if ((int64_t)(item / SUB) >= p.nitems) break;
+        const uint32_t v = p.item_vol[item / SUB];
         const BatchVol b = p.bvols[v];
-        const int64_t local = (int64_t)item - b.item0;
+        const int64_t local = (int64_t)(item / SUB) - b.item0;
         const int ty = (int)(local % b.tiles_y);
         const int tx = (int)((local / b.tiles_y) % b.tiles_x);
         const int seg = (int)(local / ((int64_t)b.tiles_y * b.tiles_x));
-        compact_tile<T>(vol_view(p, b), sm, w, lane, tx, ty, seg, v);
+        compact_tile<T, CR>(vol_view(p, b), sm, w, lane, tx, ty * SUB + (int)(item % SUB), seg, v);
     }
 }
 
@@ -254,7 +267,7 @@ template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cu
         grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>, XW);
     }
     if (stage == 0) {
-        const int nitems = p.tiles_x * p.tiles_y * p.nseg;
+        const int nitems = p.tiles_x * ((p.cy + CR - 1) / CR) * p.nseg;
         cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
         k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);
@@ -283,7 +296,7 @@ int persistent_ctas(const void *fn, int threads, int ctas_per_sm) {
 
 template <class T> cudaError_t compact_batch_t(const Plan &p, int ctas, cudaStream_t s) {
     const int grid = (int)std::min<int64_t>(persistent_ctas((const void *)k_compact_batch<T>, 32 * WARPS, ctas),
-                                            (p.nitems + WARPS - 1) / WARPS);
+                                            (p.nitems * (WY / CR) + WARPS - 1) / WARPS);
     cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
     if (e != cudaSuccess || grid < 1) return e;
     k_compact_batch<T><<<grid, 32 * WARPS, 0, s>>>(p);

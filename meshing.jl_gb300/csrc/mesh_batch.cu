@@ -125,7 +125,8 @@ int build_plan(mesh_batch *b) {
     for (int v = 0; v < n; v++) b->hv[v].vol = b->vols[v];
     const int64_t items = z.items, pieces = z.pieces, nflags = z.nflags, tdoubles = z.tdoubles, stiles = z.stiles;
     const int64_t max_ntab = z.max_ntab;
-    if (items >= ((int64_t)1 << 31) || stiles >= ((int64_t)1 << 31))
+    // the compaction splits each item into up to WY row tiles counted in 32 bits
+    if (items >= ((int64_t)1 << 31) / WY || stiles >= ((int64_t)1 << 31))
         return fail(c, MESH_ETOOLARGE, "batch has too many work items");
 
     cudaError_t e;

@@ -601,6 +601,7 @@ int launch_wave(mesh_server *s, Slot &sl) {
         std::vector<const Req *> rs;
         for (int64_t id : sl.groups[gi].reqs) rs.push_back(&sl.wave.at(id));
         layout_group(rs, &lays[gi]);
+        if (lays[gi].z.items >= ((int64_t)1 << 31) / WY) return MESH_ETOOLARGE;  // 32-bit compaction counter
         if (lays[gi].total > sl.groups[gi].scratch.size) return MESH_EDEVICE;  // bound violated: never launch
         sl.groups[gi].stage_off = stage;
         stage += up(lays[gi].head);
