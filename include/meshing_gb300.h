@@ -48,7 +48,14 @@ typedef enum {
 typedef enum {
     MESH_ALG_MC = 0,  /* MarchingCubes       (src/algorithmtypes.jl:23-25) */
     MESH_ALG_MT = 1,  /* MarchingTetrahedra  (src/algorithmtypes.jl:37-40) */
-    MESH_ALG_NSN = 2  /* NaiveSurfaceNets    (defined by this project) */
+    MESH_ALG_NSN = 2, /* NaiveSurfaceNets    (defined by this project) */
+    /* MarchingCubes with one vertex per crossed lattice edge (opt-in, not a
+     * drop-in: the reference pushes a vertex per cell and edge,
+     * src/marching_cubes.jl:72-79).  Vertices are numbered when their edge is
+     * first met -- cells in the reference's emission order, a cell's edges in
+     * its vertex-slot order -- and placed by that cell's vertex_interp; faces
+     * are the reference's triangles on those ids.  mesh_count / mesh_fill only. */
+    MESH_ALG_MC_WELDED = 3
 } mesh_alg;
 
 typedef enum {

@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, '_build', 'libmeshing_gb300.so')
 
 MESH_DT_U16, MESH_DT_F32, MESH_DT_F64, MESH_DT_I64, MESH_DT_I32, MESH_DT_F16 = 1, 2, 3, 4, 5, 6
 MESH_DT_I16, MESH_DT_I8, MESH_DT_U8 = 7, 8, 9
-MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN = 0, 1, 2
+MESH_ALG_MC, MESH_ALG_MT, MESH_ALG_NSN, MESH_ALG_MC_WELDED = 0, 1, 2, 3
 STATUS = {0: 'MESH_OK', 1: 'MESH_EINVAL', 2: 'MESH_ENOMEM', 3: 'MESH_ECUDA', 4: 'MESH_EDEVICE', 5: 'MESH_ESTATE',
           6: 'MESH_ECAPACITY', 7: 'MESH_ETOOLARGE', 8: 'MESH_ESCRATCH', 9: 'MESH_EBUDGET', 10: 'MESH_EBUSY'}
 

@@ -31,8 +31,14 @@ class AbstractMeshingAlgorithm:
 
 @dataclass(frozen=True)
 class MarchingCubes(AbstractMeshingAlgorithm):
-    """Marching Cubes; vertices are repeated per cell (src/algorithmtypes.jl:12-25)."""
+    """Marching Cubes; vertices are repeated per cell (src/algorithmtypes.jl:12-25).
+
+    ``weld=True`` (opt-in, no counterpart in the reference) gives one vertex per
+    crossed lattice edge: numbered when the edge is first met in the
+    reference's emission order, placed by that cell's vertex_interp, with the
+    reference's triangles on those ids."""
     iso: Any = 0.0
+    weld: bool = False
 
 
 @dataclass(frozen=True)
@@ -100,6 +106,8 @@ def make_params(method, X=(-1, 1), Y=(-1, 1), Z=(-1, 1)):
     p = MeshParams()
     _lib.load().mesh_params_default(ctypes.byref(p))
     p.alg = _ALG[type(method)]
+    if getattr(method, 'weld', False):
+        p.alg = _lib.MESH_ALG_MC_WELDED
     p.iso_type, p.iso = _scalar(method.iso, 'iso')
     if isinstance(method, MarchingTetrahedra):
         p.eps_type, p.eps = _scalar(method.eps, 'eps')
@@ -237,8 +245,8 @@ def isosurface_slabs(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), slab_cells
     both sides of a slab boundary, so they are not split.
     """
     method = method or MarchingCubes()
-    if not isinstance(method, MarchingCubes):
-        raise TypeError('only MarchingCubes meshes split into x slabs')
+    if not isinstance(method, MarchingCubes) or method.weld:
+        raise TypeError('only (unwelded) MarchingCubes meshes split into x slabs')
     p = make_params(method, X, Y, Z)
     dt = _VOL_DT.get(np.dtype(A.dtype))
     if dt is None or A.ndim != 3:

@@ -87,7 +87,7 @@ int validate(mesh_ctx *c, int T, int64_t nx, int64_t ny, int64_t nz, const mesh_
     // promote(Int, Float16) is Float16: (iso - v1) / (v2 - v1) would run in Float16 arithmetic
     if (T == MESH_DT_F16 && p && p->iso_type == MESH_DT_I64)
         return fail(c, MESH_EINVAL, "Float16 volumes take a Float32 or Float64 iso");
-    if (p->alg != MESH_ALG_MC && p->alg != MESH_ALG_MT && p->alg != MESH_ALG_NSN)
+    if (p->alg != MESH_ALG_MC && p->alg != MESH_ALG_MT && p->alg != MESH_ALG_NSN && p->alg != MESH_ALG_MC_WELDED)
         return fail(c, MESH_EINVAL, "unknown algorithm %d", p->alg);
     if (p->iso_type != MESH_DT_F32 && p->iso_type != MESH_DT_F64 && p->iso_type != MESH_DT_I64)
         return fail(c, MESH_EINVAL, "unsupported iso type %d", p->iso_type);
@@ -188,6 +188,9 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     P.cx = (int32_t)(nx - 1); P.cy = (int32_t)(ny - 1); P.cz = (int32_t)(nz - 1);
     set_types(P, T, p, &c->Q64, &c->A64, &c->P64);
     const int L32 = p->range_type == MESH_DT_F32;
+    // welded Marching Cubes runs the Marching Cubes kernels, then welds
+    c->weld = p->alg == MESH_ALG_MC_WELDED;
+    if (c->weld) P.alg = MESH_ALG_MC;
 
     // tiling
     P.tiles_x = (P.cx + TILE_X - 1) / TILE_X;
@@ -326,7 +329,10 @@ bool make_tensor_map(mesh_ctx *c) {
 
 // Marching Cubes walked once, classification staging the active cells (opt-in;
 // also the form that reads a mapped host volume in place).
-bool one_walk(const mesh_ctx *c) { return c->plan.alg == MESH_ALG_MC && (c->one_walk || c->host_mapped); }
+// (welded meshes need the expansion in emission order, which writes the edge keys)
+bool one_walk(const mesh_ctx *c) {
+    return c->plan.alg == MESH_ALG_MC && !c->weld && (c->one_walk || c->host_mapped);
+}
 
 int run_count(mesh_ctx *c) {
     Plan &P = c->plan;
@@ -488,8 +494,8 @@ void mesh_ctx_destroy(mesh_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->vol,   &c->tabs,  &c->cnt,   &c->base, &c->flags, &c->scan,
-                      &c->misc,  &c->out_v, &c->out_f, &c->ent,  &c->nrm};
+    DevBuf *bufs[] = {&c->vol, &c->tabs, &c->cnt,   &c->base,  &c->flags,    &c->scan,  &c->misc,
+                      &c->out_v, &c->out_f, &c->ent, &c->nrm, &c->weld_buf, &c->weld_v};
     for (DevBuf *b : bufs) b->release();
     for (auto &v : c->ev_pairs)
         for (cudaEvent_t e : v) cudaEventDestroy(e);
@@ -521,6 +527,45 @@ int mesh_output_float_bits(int T, const mesh_params *p, int *bits) {
     if (rc) return rc;
     const int tys[4] = {p->range_type, T, p->iso_type, p->eps_type};
     *bits = out_is_f64(tys, p->alg == MESH_ALG_MT ? 4 : 3) ? 64 : 32;
+    return MESH_OK;
+}
+
+// Welded Marching Cubes: extract the per-cell mesh with its edge keys into the
+// context's buffers, weld it (k_weld.cu) and keep the welded counts.
+int run_weld(mesh_ctx *c) {
+    Plan &P = c->plan;
+    const int64_t nv = c->nverts, nf = c->nfaces;
+    const size_t es = P.out64 ? 8 : 4;
+    const int64_t nb = weld_blocks(nv), hcap = weld_hash_slots(nv);
+    auto up = [](size_t n) { return (n + 255) / 256 * 256; };
+    const size_t o_bsum = up((size_t)nv * 8), o_hkey = o_bsum + up((size_t)(nb + 1) * 8),
+                 o_hval = o_hkey + up((size_t)hcap * 8), total = o_hval + up((size_t)hcap * 8);
+    cudaError_t e;
+    if ((e = c->out_v.ensure((size_t)nv * 3 * es + 16)) != cudaSuccess) return cuda_fail(c, e, "vertex buffer");
+    if ((e = c->out_f.ensure((size_t)nf * 24 + 16)) != cudaSuccess) return cuda_fail(c, e, "face buffer");
+    if ((e = c->weld_v.ensure((size_t)nv * 3 * es + 16)) != cudaSuccess) return cuda_fail(c, e, "welded vertices");
+    if ((e = c->weld_buf.ensure(total)) != cudaSuccess) return cuda_fail(c, e, "weld scratch");
+    char *wb = (char *)c->weld_buf.ptr;
+    P.verts = c->out_v.ptr;
+    P.faces = (int64_t *)c->out_f.ptr;
+    P.verts_cap = nv;
+    P.faces_cap = nf;
+    P.vkey = (long long *)wb;
+    int rc;
+    if ((rc = ensure_entries(c, c->nactive))) return rc;
+    if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
+    if ((rc = launch_emit(c))) return rc;
+    if ((e = launch_weld(P.vkey, nv, P.verts, P.out64, P.faces, nf, (long long *)(wb + o_bsum), c->weld_v.ptr,
+                         (unsigned long long *)(wb + o_hkey), (long long *)(wb + o_hval), hcap, P.err, c->sms,
+                         c->stream)) != cudaSuccess)
+        return cuda_fail(c, e, "weld launch");
+    long long nw = 0;
+    if ((e = cudaMemcpyAsync(&nw, wb + o_bsum + (size_t)nb * 8, 8, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+        return cuda_fail(c, e, "welded count");
+    if ((rc = fetch_misc(c))) return rc;  // synchronizes
+    if ((rc = check_err(c))) return rc;
+    c->nverts = nw;
+    P.vkey = nullptr;
     return MESH_OK;
 }
 
@@ -561,6 +606,7 @@ int mesh_count(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int6
     c->nverts = c->h_misc[0];
     c->nfaces = c->h_misc[1];
     c->nactive = c->h_misc[2];
+    if (c->weld && (rc = run_weld(c))) return rc;
     *nverts = c->nverts;
     *nfaces = c->nfaces;
     c->have_plan = 1;
@@ -576,6 +622,16 @@ int mesh_fill(mesh_ctx *c, void *verts, int64_t *faces, int out_on_device) {
     Plan &P = c->plan;
     const size_t vb = (size_t)c->nverts * 3 * (P.out64 ? 8 : 4), fbytes = (size_t)c->nfaces * 3 * 8;
     cudaError_t e;
+    if (c->weld) {  // the welded mesh was built by the count: copy it out
+        const cudaMemcpyKind k = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (vb && (e = cudaMemcpyAsync(verts, c->weld_v.ptr, vb, k, c->stream)) != cudaSuccess)
+            return cuda_fail(c, e, "welded vertex copy");
+        if (fbytes && (e = cudaMemcpyAsync(faces, c->out_f.ptr, fbytes, k, c->stream)) != cudaSuccess)
+            return cuda_fail(c, e, "welded face copy");
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(c, e, "synchronize");
+        c->have_plan = 0;
+        return MESH_OK;
+    }
     if (out_on_device) {
         P.verts = verts;
         P.faces = faces;
@@ -617,6 +673,7 @@ int mesh_extract_device(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t
         return MESH_OK;
     }
     if (!vol) return fail(c, MESH_EINVAL, "volume is NULL");
+    if (p->alg == MESH_ALG_MC_WELDED) return fail(c, MESH_EINVAL, "welded meshes are built by mesh_count / mesh_fill");
     if ((rc = prepare(c, vol, T, nx, ny, nz, 1, p))) return rc;
     Plan &P = c->plan;
     P.verts = verts;

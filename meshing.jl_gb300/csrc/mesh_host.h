@@ -52,6 +52,10 @@ struct mesh_ctx {
     cudaStream_t stream = nullptr;
     mesh::DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f, ent;
     mesh::DevBuf nrm;  // mesh_vertex_normals: double accumulators
+    // welded Marching Cubes (MESH_ALG_MC_WELDED): the count runs the whole
+    // extraction into out_v / out_f and welds it into weld_v; mesh_fill copies
+    int weld = 0;
+    mesh::DevBuf weld_buf, weld_v;
     int64_t *h_misc = nullptr;  // pinned: totals[NCNT], err
     mesh::Plan plan{};
     int have_plan = 0;

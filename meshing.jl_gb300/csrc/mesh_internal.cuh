@@ -80,6 +80,10 @@ struct Plan {
     int64_t *totals;      // [NCNT] total vertices, faces, active cells
     unsigned int *err;    // device error word
     unsigned int *work;   // work-item counter of the persistent kernels
+    // welded Marching Cubes: per emitted vertex, its lattice edge
+    // (axis + 3 * linear index of the edge's lower node), bit 63 set when the
+    // emitting cell is the edge's first cell in emission order (null: not written)
+    long long *vkey;
     // list of active cells (Marching Cubes): packed x | y << 21 | z << 42,
     // case, the 8 corner values; in emission order with, for every 256th
     // entry, the vertex / face offsets of that entry (ent_side), or in the
@@ -185,6 +189,15 @@ inline size_t table_bytes(int64_t ntab) {
 inline void bind_tables(Plan &P, const double *dp, int64_t nx, int64_t ny, int64_t nz) {
     set_tabs(P, tabs_at(dp, nx, ny, nz));
 }
+
+// Welded Marching Cubes (k_weld.cu): blocks of the ownership scan and hash slots
+// for nv per-cell vertices; launch_weld welds verts / faces (faces in place) into
+// wverts, bsum[nb] = the welded vertex count.
+int64_t weld_blocks(int64_t nv);
+int64_t weld_hash_slots(int64_t nv);
+cudaError_t launch_weld(const long long *vkey, int64_t nv, const void *verts, int out64, int64_t *faces, int64_t nf,
+                        long long *bsum, void *wverts, unsigned long long *hkey, long long *hval, int64_t hcap,
+                        unsigned *err, int sms, cudaStream_t s);
 
 // Launchers (each returns cudaError_t of the launch).
 // xoff / nxt: the volume is x nodes xoff .. xoff+nx-1 of an axis of nxt nodes (0, 0: the whole axis).

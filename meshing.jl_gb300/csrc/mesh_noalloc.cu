@@ -72,6 +72,7 @@ extern "C" int mesh_extract_noalloc(const void *vol, int T, int64_t nx, int64_t 
                                              const mesh_params *prm, void *verts, int64_t verts_cap, int64_t *faces,
                                              int64_t faces_cap, int64_t *counts, void *stream_handle) {
     if (!prm || !counts) return MESH_EINVAL;
+    if (prm->alg == MESH_ALG_MC_WELDED) return MESH_EINVAL;  // welding needs scratch of its own
     int bits = 0;
     int rc = mesh_output_float_bits(T, prm, &bits);  // validates types and values
     if (rc) return rc;

@@ -858,6 +858,7 @@ int mesh_server_submit(mesh_server *s, const void *vol, int vol_dtype, int64_t n
     *id = 0;
     int rc = validate(nullptr, vol_dtype, nx, ny, nz, p);
     if (rc) return sfail(s, rc, "invalid request");
+    if (p->alg == MESH_ALG_MC_WELDED) return sfail(s, MESH_EINVAL, "welded meshes are not served");
     if (!vol && nx > 1 && ny > 1 && nz > 1) return sfail(s, MESH_EINVAL, "volume is NULL");
     Req r;
     r.vol = vol;

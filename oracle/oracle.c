@@ -38,7 +38,7 @@
 #include "ref_luts.h"
 
 enum { ORC_U16 = 1, ORC_F32 = 2, ORC_F64 = 3, ORC_I64 = 4, ORC_I32 = 5, ORC_F16 = 6, ORC_I16 = 7, ORC_I8 = 8, ORC_U8 = 9 };
-enum { ORC_MC = 0, ORC_MT = 1, ORC_NSN = 2 };
+enum { ORC_MC = 0, ORC_MT = 1, ORC_NSN = 2, ORC_MCW = 3 };
 enum { ORC_OK = 0, ORC_EINVAL = 1, ORC_ENOMEM = 2 };
 
 typedef struct {
@@ -378,6 +378,61 @@ static int get_vert_id(const orc_ctx *c, imap *h, orc_mesh *m, int e, int64_t x,
 
 static const int MT_CORNER[8][3] = {{0,0,0},{0,1,0},{1,1,0},{1,0,0},{0,0,1},{0,1,1},{1,1,1},{1,0,1}};
 
+/* Welded Marching Cubes (no counterpart in the reference, whose
+ * process_mc_voxel! pushes a fresh vertex for every crossed edge of every cell,
+ * src/marching_cubes.jl:72-79): one vertex per crossed lattice edge, numbered
+ * when the edge is first met -- cells in the reference's emission order, a
+ * cell's edges in its vertex-slot order -- and placed by that first cell's
+ * vertex_interp; the faces are the reference's triangles on those ids. */
+
+static int run_mc_welded(const orc_ctx *c, orc_mesh *m) {
+    imap h = {0};
+    int rc = imap_grow(&h);
+    if (rc) return rc;
+    double v[8], p[8][3], q[3];
+    int64_t ids[12];
+    for (int64_t xi = 0; xi + 1 < c->nx && !rc; xi++)
+        for (int64_t yi = 0; yi + 1 < c->ny && !rc; yi++)
+            for (int64_t zi = 0; zi + 1 < c->nz && !rc; zi++) {
+                int ci = mc_case(c, xi, yi, zi, v);
+                if (ci == 0 || ci == 255) continue;
+                mc_points(c, xi, yi, zi, p);
+                const uint8_t *row = R_MC_VERTS[ci - 1];
+                for (int i = 0; i < 12; i++) {
+                    int vt = row[i];
+                    if (vt == 0) break;
+                    int a = R_MC_EDGE_LIST[vt - 1][0] - 1, b = R_MC_EDGE_LIST[vt - 1][1] - 1;
+                    int ax = MC_CORNER[a][0] != MC_CORNER[b][0] ? 0 : (MC_CORNER[a][1] != MC_CORNER[b][1] ? 1 : 2);
+                    int64_t lx = xi + (MC_CORNER[a][0] < MC_CORNER[b][0] ? MC_CORNER[a][0] : MC_CORNER[b][0]);
+                    int64_t ly = yi + (MC_CORNER[a][1] < MC_CORNER[b][1] ? MC_CORNER[a][1] : MC_CORNER[b][1]);
+                    int64_t lz = zi + (MC_CORNER[a][2] < MC_CORNER[b][2] ? MC_CORNER[a][2] : MC_CORNER[b][2]);
+                    int64_t key = ax + 3 * (lx + c->nx * (ly + c->ny * lz));
+                    if (2 * (h.n + 1) > h.cap && (rc = imap_grow(&h))) break;
+                    int64_t sl = imap_slot(&h, key);
+                    if (h.keys[sl] == key) {
+                        ids[i] = h.vals[sl];
+                        continue;
+                    }
+                    vertex_interp(c, p[a], p[b], v[a], v[b], q);
+                    if ((rc = push_vert(m, q))) break;
+                    h.keys[sl] = key;
+                    h.vals[sl] = m->nverts;  /* 1-based */
+                    h.n++;
+                    ids[i] = m->nverts;
+                }
+                if (rc) break;
+                const uint8_t *o = R_MC_CONNECTIVITY[R_MC_EQ_MAPPING[ci - 1] - 1];
+                if ((rc = push_face(m, ids[2], ids[1], ids[0]))) break;
+                for (int i = 0; i < 12; i += 3) {
+                    if (o[i] == 0) break;
+                    if ((rc = push_face(m, ids[o[i + 2] - 1], ids[o[i + 1] - 1], ids[o[i] - 1]))) break;
+                }
+            }
+    free(h.keys);
+    free(h.vals);
+    return rc;
+}
+
 static int run_mt(const orc_ctx *c, orc_mesh *m) {
     imap h = {0};
     int rc = imap_grow(&h);
@@ -533,6 +588,7 @@ int orc_isosurface(const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, i
     if (!rc) {
         out->out_bits = c.O == ORC_F32 ? 32 : 64;
         if (alg == ORC_MC) rc = run_mc(&c, out);
+        else if (alg == ORC_MCW) rc = run_mc_welded(&c, out);
         else if (alg == ORC_MT) rc = run_mt(&c, out);
         else if (alg == ORC_NSN) rc = run_nsn(&c, out);
         else rc = ORC_EINVAL;

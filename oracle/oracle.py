@@ -19,7 +19,7 @@ LIB = os.path.join(BUILD, 'liborc.so')
 SRC = [os.path.join(HERE, 'oracle.c'), os.path.join(HERE, 'ref_luts.h')]
 
 U16, F32, F64, I64, I32, F16, I16, I8, U8 = 1, 2, 3, 4, 5, 6, 7, 8, 9
-ALGS = {'mc': 0, 'mt': 1, 'nsn': 2}
+ALGS = {'mc': 0, 'mt': 1, 'nsn': 2, 'mcw': 3}
 DTYPES = {np.dtype(np.uint16): U16, np.dtype(np.float32): F32, np.dtype(np.float64): F64, np.dtype(np.int64): I64,
           np.dtype(np.int32): I32, np.dtype(np.float16): F16, np.dtype(np.int16): I16, np.dtype(np.int8): I8,
           np.dtype(np.uint8): U8}

@@ -264,3 +264,31 @@ def test_float16_volumes(pkg, oracle, cuda, alg):
     for iso in (np.float32(0), 1.0e4, np.float32(-2.5e4)):
         check(pkg, oracle, big, alg, iso, np.float32(1e-3) if isinstance(iso, np.float32) else 1e-3)
     check(pkg, oracle, big, alg, 0.0, 1e-3, ((np.float32(-2), np.float32(3)),) * 3, device=True)
+
+
+@pytest.mark.parametrize('case', range(len(TYPE_CASES)))
+def test_welded_marching_cubes(pkg, oracle, cuda, case):
+    # MarchingCubes(weld=True): one vertex per crossed lattice edge in first-touch order,
+    # against the oracle's welded restatement, on random grids of every type and on a
+    # shape spanning several tiles / segments; host and device volumes
+    dt, iso, eps, r = TYPE_CASES[case]
+    rng = np.random.default_rng(300 + case)
+    for trial in range(3):
+        shape = tuple(int(s) for s in rng.integers(2, 18, 3))
+        A = rng.integers(0, 1000, shape).astype(np.uint16) if dt == np.uint16 else rng.standard_normal(shape).astype(dt)
+        A = np.asfortranarray(A)
+        want = oracle.isosurface(A, 'mcw', iso, eps, (r, r, r))
+        got = pkg.isosurface(A, pkg.MarchingCubes(iso=iso, weld=True), r, r, r)
+        assert_same(got, want, 'welded %s %s' % (dt, shape))
+    B = sphere(0, 0.6, np.float32, c=(0.05, -0.1, 0.02), shape=(67, 45, 133)).astype(dt) if dt != np.uint16 else \
+        np.asfortranarray((sphere(0, 0.6, np.float64, shape=(67, 45, 133)) * 1000 + 500).astype(np.uint16))
+    want = oracle.isosurface(B, 'mcw', iso, eps, (r, r, r))
+    m = pkg.MarchingCubes(iso=iso, weld=True)
+    assert_same(pkg.isosurface(B, m, r, r, r), want, 'welded sphere')
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(B.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+    v, f = pkg.isosurface(t, m, r, r, r)
+    torch.cuda.synchronize()
+    assert_same((v.cpu().numpy(), f.cpu().numpy()), want, 'welded sphere, device volume')
+    plain = oracle.isosurface(B, 'mc', iso, eps, (r, r, r))
+    assert len(want[0]) < len(plain[0]) and len(want[1]) == len(plain[1])

@@ -230,3 +230,47 @@ def test_float16_volume_eltype_rule(oracle, iso, rt, bits):
     for alg in ('mc', 'mt'):
         eps = np.float32(1e-3) if bits == 32 else 1e-3
         assert oracle.output_bits(np.float16, alg, iso, eps, rt) == bits
+
+
+def test_mc_case_table_puts_a_vertex_on_every_crossed_edge():
+    # the welded mode numbers vertices by lattice edge: it relies on every case's vertex
+    # slots being exactly its crossed edges (src/lut/mc.jl tables, through ref_luts.h)
+    T = pyoracle._T
+    corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    edges = [tuple(int(t) - 1 for t in T['R_MC_EDGE_LIST'][k]) for k in range(12)]
+    for ci in range(1, 255):
+        slots = [int(s) for s in T['R_MC_VERTS'][ci - 1] if s]
+        crossed = {k for k, (a, b) in enumerate(edges) if ((ci >> a) & 1) != ((ci >> b) & 1)}
+        assert sorted(s - 1 for s in slots) == sorted(crossed), ci
+        assert len(slots) == len(set(slots))
+    assert all(sum(abs(corner[a][i] - corner[b][i]) for i in range(3)) == 1 for a, b in edges)
+
+
+@pytest.mark.parametrize('dt,iso', [(np.float64, 0.0), (np.float32, np.float32(0.1)), (np.uint16, 500)])
+def test_welded_mc_is_the_deduplicated_mesh(oracle, dt, iso):
+    rng = np.random.default_rng(4)
+    for trial in range(4):
+        sh = tuple(int(s) for s in rng.integers(2, 12, 3))
+        A = rng.integers(0, 1000, sh).astype(dt) if dt == np.uint16 else rng.standard_normal(sh).astype(dt)
+        A = np.asfortranarray(A)
+        uv, uf = oracle.isosurface(A, 'mc', iso)
+        wv, wf = oracle.isosurface(A, 'mcw', iso)
+        assert wf.shape == uf.shape and wv.dtype == uv.dtype
+        # every welded vertex is the unwelded vertex where its edge first appears: the
+        # welded list is an ordered subsequence of the unwelded one
+        k = 0
+        for j in range(len(uv)):
+            if k < len(wv) and np.array_equal(uv[j], wv[k]):
+                k += 1
+        assert k == len(wv)
+        # faces name the same corners: welded face vertices equal the unwelded ones, to
+        # rounding where a later cell met the edge from its other end (UInt16 differences
+        # wrap differently from the two ends, so there only the first cell's vertex counts)
+        if dt != np.uint16:
+            assert np.allclose(wv[wf - 1], uv[uf - 1], rtol=0, atol=1e-6)
+        assert len(wv) <= len(uv) and (len(uv) == 0 or len(wv) < len(uv) or trial >= 0)
+        # welded ids are numbered by first use in the face list's order of cells
+        assert wf.min(initial=1) >= 1 and wf.max(initial=0) == len(wv)
+        used = np.unique(wf)
+        assert len(used) == len(wv)
+        assert set(np.arange(1, len(wv) + 1)) == set(used.tolist())
