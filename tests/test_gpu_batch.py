@@ -81,14 +81,23 @@ def test_knobs_graph_and_tuner_keep_results(pkg, cuda):
     b.close()
 
 
-@pytest.mark.parametrize('dt', ['f64', 'u16'])
+@pytest.mark.parametrize('dt', ['f64', 'u16', 'f16', 'i16', 'u8'])
 def test_batch_dtypes_and_per_volume_ranges(pkg, cuda, dt):
     torch = cuda
     rng = np.random.default_rng(5)
+    shapes = [tuple(int(s) for s in rng.integers(3, 40, 3)) for _ in range(25)]
     if dt == 'u16':
-        vols = [(torch.rand(tuple(int(s) for s in rng.integers(3, 40, 3)), device='cuda') * 1000).to(torch.int32)
-                .to(torch.uint16) for _ in range(25)]
+        vols = [(torch.rand(sh, device='cuda') * 1000).to(torch.int32).to(torch.uint16) for sh in shapes]
         m = pkg.MarchingCubes(iso=500)
+    elif dt == 'i16':
+        vols = [(torch.rand(sh, device='cuda') * 2000 - 1000).to(torch.int16) for sh in shapes]
+        m = pkg.MarchingCubes(iso=7)
+    elif dt == 'u8':
+        vols = [(torch.rand(sh, device='cuda') * 255).to(torch.uint8) for sh in shapes]
+        m = pkg.MarchingCubes(iso=np.float32(99.5))
+    elif dt == 'f16':
+        vols = ragged(torch, 25, 3, 3, 40, torch.float16)
+        m = pkg.MarchingCubes(iso=np.float32(0.01))
     else:
         vols = ragged(torch, 25, 3, 3, 40, torch.float64)
         m = pkg.MarchingCubes(iso=0.01)

@@ -140,3 +140,28 @@ def test_bursts_and_concurrent_submitters(pkg, cuda):
             assert same(torch, srv.result(rid), want[i])
             srv.release(rid)
     srv.close()
+
+
+def test_small_int_and_float16_requests(pkg, cuda):
+    # Float16 / Int16 / UInt8 / Int8 volumes through the serving loop, every algorithm,
+    # equal to the volume's own isosurface call; welded meshes are not served
+    torch = cuda
+    rng = np.random.default_rng(9)
+    vols = [
+        (torch.rand((21, 30, 17), device='cuda').to(torch.float16), np.float32(0.5)),
+        ((torch.rand((25, 19, 33), device='cuda') * 2000 - 1000).to(torch.int16), 0),
+        ((torch.rand((18, 27, 22), device='cuda') * 255).to(torch.uint8), 128),
+        ((torch.rand((23, 23, 23), device='cuda') * 250 - 125).to(torch.int8), np.float32(0.5)),
+    ]
+    srv = pkg.Server(budget_bytes=2 << 30)
+    for A, iso in vols:
+        for m in (pkg.MarchingCubes(iso=iso), pkg.MarchingTetrahedra(iso=iso, eps=np.float32(1e-3)),
+                  pkg.NaiveSurfaceNets(iso=iso)):
+            want = pkg.isosurface(A, m)
+            rid = srv.submit(A, m)
+            assert same(torch, srv.result(rid), want), (A.dtype, type(m).__name__)
+            srv.release(rid)
+    with pytest.raises(pkg.MeshError):
+        srv.submit(vols[0][0], pkg.MarchingCubes(iso=np.float32(0.5), weld=True))
+    srv.close()
+    del rng
