@@ -155,7 +155,8 @@ MESH_API int mesh_vertex_normals(mesh_ctx *ctx, const void *verts, int float_bit
  * stage -- 0 classify, 1 scan, 2 emit (the Marching Cubes active-cell
  * compaction, or the whole MT / NSN emit), 3 Marching Cubes expansion -- the
  * summed device milliseconds ms[0..3] and the number of kernel launches
- * launches[0..3] since the previous query, then resets. */
+ * launches[0..3] since the previous query (the coordinate-table kernel counts
+ * with stage 0, the four scan kernels with stage 1), then resets. */
 MESH_API int mesh_ctx_enable_timing(mesh_ctx *ctx, int enable);
 MESH_API int mesh_ctx_stage_times(mesh_ctx *ctx, double *ms, int64_t *launches);
 

@@ -179,6 +179,8 @@ void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P6
 
 namespace {
 
+void count_kernels(mesh_ctx *c, int stage, int n);
+
 int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
             const mesh_params *p) {
     Plan &P = c->plan;
@@ -236,6 +238,7 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     if ((e = launch_tables((double *)c->tabs.ptr, nx, ny, nz, p->range, L32, c->stream, c->win_x0, c->win_nx)) !=
         cudaSuccess)
         return cuda_fail(c, e, "table launch");
+    count_kernels(c, 0, 1);  // the coordinate tables count with the classification
     bind_tables(P, (double *)c->tabs.ptr, nx, ny, nz);
     P.force_fp64 = c->force_fp64;
 
@@ -275,6 +278,11 @@ cudaEvent_t take_event(mesh_ctx *c) {
         return nullptr;
     }
     return e;
+}
+
+// With timing on: kernels launched in `stage` (for mesh_ctx_stage_times).
+void count_kernels(mesh_ctx *c, int stage, int n) {
+    if (c->timing) c->nkern[stage] += n;
 }
 
 void mark(mesh_ctx *c, int stage) {
@@ -345,9 +353,11 @@ int run_count(mesh_ctx *c) {
     else e = c->use_tma ? launch_classify_tma(P, c->tmap, c->stream) : launch_classify(P, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "classify launch");
     mark(c, 0);
+    count_kernels(c, 0, 1);
     mark(c, 1);
     if ((e = launch_scan(P, c->stream)) != cudaSuccess) return cuda_fail(c, e, "scan launch");
     mark(c, 1);
+    count_kernels(c, 1, 4);  // reduce, column scan, column-sum scan, downsweep
     return MESH_OK;
 }
 
@@ -399,17 +409,20 @@ int launch_emit(mesh_ctx *c) {
         mark(c, 3);
         e = launch_expand_staged_mc(c->plan, c->Q64, c->P64, c->stream);
         mark(c, 3);
+        count_kernels(c, 3, 1);
         return e != cudaSuccess ? cuda_fail(c, e, "expand launch") : MESH_OK;
     }
     mark(c, 2);
     if (c->plan.alg == MESH_ALG_MC) e = launch_emit_mc(c->plan, c->Q64, c->P64, 0, c->stream);
     else e = launch_emit_halo(c->plan, c->Q64, c->A64, c->P64, c->stream);
     mark(c, 2);
+    count_kernels(c, 2, 1);
     if (e != cudaSuccess) return cuda_fail(c, e, "emit launch");
     if (c->plan.alg == MESH_ALG_MC) {
         mark(c, 3);
         e = launch_emit_mc(c->plan, c->Q64, c->P64, 1, c->stream);
         mark(c, 3);
+        count_kernels(c, 3, 1);
         if (e != cudaSuccess) return cuda_fail(c, e, "expand launch");
     }
     return MESH_OK;
@@ -722,8 +735,9 @@ int mesh_ctx_stage_times(mesh_ctx *c, double *ms, int64_t *launches) {
             if (e == cudaSuccess) e = cudaEventElapsedTime(&t, v[i], v[i + 1]);
             if (e != cudaSuccess) rc = cuda_fail(c, e, "stage timing");
             ms[s] += t;
-            launches[s]++;
         }
+        launches[s] = c->nkern[s];
+        c->nkern[s] = 0;
         for (cudaEvent_t e : v) c->ev_free.push_back(e);
         v.clear();
     }

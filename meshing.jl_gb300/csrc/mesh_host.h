@@ -89,6 +89,7 @@ struct mesh_ctx {
     CUtensorMap tmap;
     std::vector<cudaEvent_t> ev_free;
     std::vector<cudaEvent_t> ev_pairs[mesh::NSTAGE];  // start, stop, start, stop, ...
+    int64_t nkern[mesh::NSTAGE] = {};                 // kernels launched per stage (with timing on)
 };
 
 namespace mesh {
