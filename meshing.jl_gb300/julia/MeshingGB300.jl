@@ -21,7 +21,7 @@ module MeshingGB300
 using Meshing
 import Meshing: isosurface, MarchingCubes, MarchingTetrahedra, AbstractMeshingAlgorithm
 
-export NaiveSurfaceNets
+export NaiveSurfaceNets, WeldedMarchingCubes
 
 const libmesh = joinpath(@__DIR__, "..", "_build", "libmeshing_gb300.so")
 
@@ -32,6 +32,18 @@ One vertex per cell straddling `iso` (mean of its edge crossings) and two
 triangles per crossed lattice edge, joining the four cells around it.
 """
 Base.@kwdef struct NaiveSurfaceNets{T} <: AbstractMeshingAlgorithm
+    iso::T = 0.0
+end
+
+"""
+    WeldedMarchingCubes(; iso=0.0)
+
+Marching Cubes with one vertex per crossed lattice edge (opt-in, not a drop-in
+for `MarchingCubes`): vertices numbered when their edge is first met in the
+reference's emission order and placed by that cell's `vertex_interp`; faces are
+`MarchingCubes`' triangles on those vertices.
+"""
+Base.@kwdef struct WeldedMarchingCubes{T} <: AbstractMeshingAlgorithm
     iso::T = 0.0
 end
 
@@ -130,6 +142,13 @@ function isosurface(sdf::Array{T,3}, method::NaiveSurfaceNets{I}, X=-1:1, Y=-1:1
     device_ok(T, I) || error("NaiveSurfaceNets: Float16 volumes take a Float32 or Float64 iso")
     FT = promote_type(eltype(first(X)), eltype(first(Y)), eltype(first(Z)), T, I)
     device_isosurface(sdf, Int32(2), method.iso, 1e-3, X, Y, Z, float(FT))
+end
+
+function isosurface(sdf::Array{T,3}, method::WeldedMarchingCubes{I}, X=-1:1, Y=-1:1, Z=-1:1) where {T<:DevEl,I<:DevScalar}
+    supported(X, Y, Z) || error("WeldedMarchingCubes: range endpoints must share one of Float32, Float64, Int64")
+    device_ok(T, I) || error("WeldedMarchingCubes: Float16 volumes take a Float32 or Float64 iso")
+    FT = promote_type(eltype(first(X)), eltype(first(Y)), eltype(first(Z)), T, I)
+    device_isosurface(sdf, Int32(3), method.iso, 1e-3, X, Y, Z, float(FT))
 end
 
 end # module
