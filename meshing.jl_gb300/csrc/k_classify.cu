@@ -461,7 +461,10 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
     __shared__ uint32_t s_tab[256];
     __shared__ __align__(8) uint64_t full[TMA_STAGES], empty[TMA_STAGES];
     __shared__ int s_fail;
-    load_tables<ALG>(s_tab);
+    if (ALG == MESH_ALG_MC)
+        load_tables_mc_packed(s_tab);
+    else
+        load_tables<ALG>(s_tab);
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int tx = blockIdx.x, seg = blockIdx.z;
@@ -512,8 +515,13 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
 #pragma unroll
         for (int r = 0; r <= WY; r++) rowok[r] = xs < p.nx && y0 + r < p.ny;
         Counts<WY> c;
+        uint32_t pk[WY], rmask[WY];  // Marching Cubes: packed words of the current chunk
 #pragma unroll
-        for (int r = 0; r < WY; r++) c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
+        for (int r = 0; r < WY; r++) {
+            c.v[r] = c.f[r] = c.a[r] = c.act[r] = 0;
+            pk[r] = 0;
+            rmask[r] = (cellx && y0 + r < p.cy) ? 0xffffffffu : 0u;
+        }
         const uint32_t xval = __ballot_sync(FULL, xs < p.nx);
         const uint32_t cellm = __ballot_sync(FULL, cellx);
         uint32_t mlo[WY + 1];
@@ -541,8 +549,39 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
                                              rowok[r] && below(st[k * PLANE + (w * WY + r) * BX + xoff + lane], p));
                     if (plane > zbeg) {
                         const int zc = plane - 1;
-                        step<ALG, WY>(p, s_tab, mlo, m, xval, cellm, lane, xs, y0, zc, c);
-                        chunk_end(p, lane, tx, y0, seg, zbeg, zc, zend, c);
+                        if (ALG == MESH_ALG_MC) {  // packed words, as classify_tile_mc
+                            uint32_t all1 = xval, any1 = 0;
+#pragma unroll
+                            for (int r = 0; r <= WY; r++) {
+                                all1 &= mlo[r] & m[r];
+                                any1 |= mlo[r] | m[r];
+                            }
+                            if (all1 != xval && any1 != 0u) {
+                                uint32_t nb[WY + 1];
+#pragma unroll
+                                for (int r = 0; r <= WY; r++) nb[r] = row_field(mlo[r], m[r], lane);
+#pragma unroll
+                                for (int r = 0; r < WY; r++) pk[r] += s_tab[nb[r] | (nb[r + 1] << 4)] & rmask[r];
+                            }
+                            if (((zc + 1 - zbeg) % ZC) == 0 || zc + 1 == zend) {
+                                const int chunk = seg * p.chunks_per_seg + (zc - zbeg) / ZC;
+                                uint8_t mine = 0;
+#pragma unroll
+                                for (int r = 0; r < WY; r++) {
+                                    const bool act = __any_sync(FULL, pk[r] != 0u);
+                                    if (lane == r) mine = act;
+                                    c.v[r] += pk[r] & ((1u << PK_F) - 1u);
+                                    c.f[r] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
+                                    c.a[r] += pk[r] >> PK_A;
+                                    pk[r] = 0;
+                                }
+                                if (lane < WY && y0 + lane < p.cy)
+                                    p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+                            }
+                        } else {
+                            step<ALG, WY>(p, s_tab, mlo, m, xval, cellm, lane, xs, y0, zc, c);
+                            chunk_end(p, lane, tx, y0, seg, zbeg, zc, zend, c);
+                        }
                     }
 #pragma unroll
                     for (int r = 0; r <= WY; r++) mlo[r] = m[r];
