@@ -173,8 +173,8 @@ def _split_args(args):
 def isosurface(A, *args, ctx=None):
     """isosurface(A[, method][, X, Y, Z]) -> (points, faces).
 
-    ``A``: 3-D numpy array or torch tensor indexed [x, y, z], eltype UInt16, Int32, Int64,
-    Float32 or Float64.  numpy (and CPU torch) inputs return numpy arrays;
+    ``A``: 3-D numpy array or torch tensor indexed [x, y, z], eltype UInt8, Int8, Int16,
+    UInt16, Int32, Int64, Float16, Float32 or Float64.  numpy (and CPU torch) inputs return numpy arrays;
     CUDA torch inputs return CUDA torch tensors: points (V, 3) of float(FT)
     and faces (F, 3) int64, 1-based.
     """

@@ -292,3 +292,26 @@ def test_welded_marching_cubes(pkg, oracle, cuda, case):
     assert_same((v.cpu().numpy(), f.cpu().numpy()), want, 'welded sphere, device volume')
     plain = oracle.isosurface(B, 'mc', iso, eps, (r, r, r))
     assert len(want[0]) < len(plain[0]) and len(want[1]) == len(plain[1])
+
+
+def _golden_cases():
+    from test_golden import CASES
+    return CASES
+
+
+@pytest.mark.parametrize('idx', range(25))
+def test_golden_fixtures(pkg, cuda, idx):
+    # the committed golden meshes (tests/golden, oracle outputs frozen by make_golden.py):
+    # the CUDA path reproduces them byte for byte, from host and from device volumes
+    import torch
+    cases = _golden_cases()
+    if idx >= len(cases):
+        pytest.skip('fewer golden cases')
+    m, vol, v, f, iso, eps, ranges = cases[idx]
+    alg = m['alg']
+    meth = pkg.MarchingCubes(iso=iso, weld=True) if alg == 'mcw' else method(pkg, alg, iso, eps)
+    assert_same(pkg.isosurface(vol, meth, *ranges), (v, f), m['name'])
+    t = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+    gv, gf = pkg.isosurface(t, meth, *ranges)
+    torch.cuda.synchronize()
+    assert_same((gv.cpu().numpy(), gf.cpu().numpy()), (v, f), m['name'] + ' (device volume)')
