@@ -66,7 +66,8 @@ typedef enum {
     MESH_EDEVICE = 4,      /* a kernel reported an error (bounded wait expired, bounds check) */
     MESH_ESTATE = 5,       /* mesh_fill without a preceding successful mesh_count */
     MESH_ECAPACITY = 6,    /* output buffers smaller than the mesh */
-    MESH_ETOOLARGE = 7,    /* volume beyond the engine's index limits (more than 2^21 samples on an axis) */
+    MESH_ETOOLARGE = 7,    /* volume beyond the engine's index limits (more than 2^21 samples on x or z,
+                              more than 2^21 - 31 on y) */
     MESH_ESCRATCH = 8,     /* mesh_extract_noalloc: the call needs more than MESH_NOALLOC_SCRATCH_BYTES */
     MESH_EBUDGET = 9,      /* mesh_server_submit: the request's worst case exceeds the memory budget */
     MESH_EBUSY = 10        /* mesh_server_submit: the queue is full */

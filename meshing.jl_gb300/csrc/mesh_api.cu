@@ -208,7 +208,7 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     P.chunks_per_seg = zs / ZC;
     P.nchunks = P.nseg * P.chunks_per_seg;
     if ((P.tiles_y + WARPS - 1) / WARPS > 65535 || P.nseg > 65535)
-        return fail(c, MESH_ETOOLARGE, "grid too large for this volume shape");
+        return fail(c, MESH_ETOOLARGE, "grid too large for this volume shape (at most 2^21 - 31 samples on y)");
 
     cudaError_t e;
     const size_t es = dtype_size(T);

@@ -315,3 +315,25 @@ def test_golden_fixtures(pkg, cuda, idx):
     gv, gf = pkg.isosurface(t, meth, *ranges)
     torch.cuda.synchronize()
     assert_same((gv.cpu().numpy(), gf.cpu().numpy()), (v, f), m['name'] + ' (device volume)')
+
+
+@pytest.mark.parametrize('axis', [0, 1, 2])
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_maximum_axis_length(pkg, oracle, cuda, alg, axis):
+    # the longest axis the engine takes: 2^21 samples on x and z (cell coordinates are
+    # packed in 21 bits), 2^21 - 31 on y (65535 CTA rows of 32 cell rows in the launch
+    # grid); one sample more is MESH_ETOOLARGE
+    n = (1 << 21) - (31 if axis == 1 else 0)
+    shape = [3, 3, 3]
+    shape[axis] = n
+    line = np.cos(2 * np.pi * np.arange(n) / 1000.0)
+    a, b = np.meshgrid([0.0, 0.15, 0.3], [0.0, -0.1, -0.2], indexing='ij')
+    along = np.moveaxis(line[:, None, None] + a[None] + b[None], 0, axis)
+    A = np.asfortranarray(along.astype(np.float32))
+    assert A.shape == tuple(shape)
+    v, f = check(pkg, oracle, A, alg, iso=np.float32(0.1))
+    assert len(f) > 4000
+    shape[axis] += 1
+    with pytest.raises(pkg.MeshError) as ei:
+        pkg.isosurface(np.zeros(shape, np.float32, order='F'), method(pkg, alg, np.float32(0.1)))
+    assert ei.value.status == 7  # MESH_ETOOLARGE
