@@ -128,6 +128,40 @@ def measured_peak():
         return 6800.0, 'fallback'
 
 
+def _spread(xs):
+    """min / median / p90 / max / mean of a list of step times (ms)."""
+    if not xs:
+        return None
+    ys = sorted(xs)
+    q = lambda f: ys[min(len(ys) - 1, int(f * len(ys)))]
+    return {'min': ys[0], 'median': q(0.5), 'p90': q(0.9), 'max': ys[-1], 'mean': sum(ys) / len(ys)}
+
+
+def host_link(hvol, hv, hf, dev):
+    """Copy-engine throughput (GB/s) of the end-to-end run's own pinned buffers: the
+    volume up, the mesh down; best of 3, CUDA events."""
+    import torch
+    dvol = torch.empty(hvol.shape, dtype=hvol.dtype, device=dev)
+    dv = torch.empty(hv.shape, dtype=hv.dtype, device=dev)
+    df = torch.empty(hf.shape, dtype=hf.dtype, device=dev)
+    out = {}
+    for key, pairs in (('h2d_gbs', ((dvol, hvol),)), ('d2h_gbs', ((hv, dv), (hf, df)))):
+        nbytes = sum(src.numel() * src.element_size() for _, src in pairs)
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for dst, src in pairs:
+                dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[key] = nbytes / (best * 1e-3) / 1e9
+    del dvol, dv, df
+    return out
+
+
 def cpu_baseline(n, planes, steps=1, warmup=0):
     """Oracle (CPU restatement of MarchingCubes) on a z slab of the field: Gvoxels/s."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
@@ -225,24 +259,31 @@ def run_ours(args, rank, world, dist):
     hf = torch.empty((nf, 3), dtype=torch.int64, pin_memory=True)
     ctx.set_stream(None)
 
+    split = []  # per step: (mesh_count ms, mesh_fill ms), host clock
+
     def e2e_step():
         a, b = ctypes.c_int64(), ctypes.c_int64()
+        t0 = time.perf_counter()
         pkg._lib.check(lib.mesh_count(ctx.handle, ctypes.c_void_p(hvol.data_ptr()), 2, n, n, n, 0, ctypes.byref(p),
                                       ctypes.byref(a), ctypes.byref(b)), ctx.handle)
+        t1 = time.perf_counter()
         pkg._lib.check(lib.mesh_fill(ctx.handle, ctypes.c_void_p(hv.data_ptr()), ctypes.c_void_p(hf.data_ptr()), 0),
                        ctx.handle)
+        split.append(((t1 - t0) * 1e3, (time.perf_counter() - t1) * 1e3))
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    split.clear()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     ok = torch.equal(hv.to(dev), verts) and torch.equal(hf.to(dev), faces)
+    link = host_link(hvol, hv, hf, dev)  # overwrites hv / hf: after the check
 
     if dist:
         t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=dev)
@@ -303,7 +344,9 @@ def run_ours(args, rank, world, dist):
         'kernels': kern,
         'pipeline': {'bytes': in_b + out_b, 'achieved': pipe_gbs, 'frac': pipe_gbs / peak, 'unit': 'GB/s'},
         'e2e': {'value': vox * world / (e2e_ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': e2e_ms,
-                'h2d_bytes_per_step': int(in_b), 'd2h_bytes_per_step': int(out_b)},
+                'h2d_bytes_per_step': int(in_b), 'd2h_bytes_per_step': int(out_b),
+                'count_ms': _spread([c for c, _ in split]), 'fill_ms': _spread([f for _, f in split]),
+                'link': link, 'link_bound_ms': (in_b / link['h2d_gbs'] + out_b / link['d2h_gbs']) / 1e6},
         'gpu_launches': int(sum(v[1] for v in st.values())),
         'cpu_baseline': cpu,
         'clocks': ck,

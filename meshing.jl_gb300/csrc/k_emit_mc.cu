@@ -222,6 +222,7 @@ __global__ void __launch_bounds__(256, COMPACT_MIN_CTAS) k_compact_mc(const Plan
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int tiles_y = (p.cy + CR - 1) / CR;
+    const int ntx = p.ntx > 0 ? p.ntx : p.tiles_x;  // x tiles tx0 .. tx0 + ntx - 1
     // persistent warps: take (y tile, x tile, segment) items in order from a counter
     for (;;) {
         int item = 0;
@@ -229,8 +230,8 @@ __global__ void __launch_bounds__(256, COMPACT_MIN_CTAS) k_compact_mc(const Plan
         item = __shfl_sync(FULL, item, 0);
         if (item >= nitems) break;
         const int ty = item % tiles_y;
-        const int tx = (item / tiles_y) % p.tiles_x;
-        const int seg = item / (tiles_y * p.tiles_x);
+        const int tx = p.tx0 + (item / tiles_y) % ntx;
+        const int seg = item / (tiles_y * ntx);
         compact_tile<T, CR>(p, sm, w, lane, tx, ty, seg, 0);
     }
 }
@@ -267,7 +268,7 @@ template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cu
         grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>, XW);
     }
     if (stage == 0) {
-        const int nitems = p.tiles_x * ((p.cy + CR - 1) / CR) * p.nseg;
+        const int nitems = (p.ntx > 0 ? p.ntx : p.tiles_x) * ((p.cy + CR - 1) / CR) * p.nseg;
         cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
         k_compact_mc<T><<<std::min(grid_a, (nitems + WARPS - 1) / WARPS), 32 * WARPS, 0, s>>>(p, nitems);

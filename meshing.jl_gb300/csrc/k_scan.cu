@@ -449,4 +449,18 @@ cudaError_t launch_scan(const Plan &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// ---- a few prefix values for the host (the pipelined host path's split points) ----
+
+namespace {
+__global__ void k_gather(const int64_t *src, const GatherIdx g, int64_t *dst) {
+    if ((int)threadIdx.x < g.n) dst[threadIdx.x] = src[g.idx[threadIdx.x]];
+}
+}  // namespace
+
+cudaError_t launch_gather(const int64_t *src, const GatherIdx &g, int64_t *dst, cudaStream_t s) {
+    if (g.n < 1 || g.n > GATHER_MAX) return cudaErrorInvalidValue;
+    k_gather<<<1, GATHER_MAX, 0, s>>>(src, g, dst);
+    return cudaGetLastError();
+}
+
 }  // namespace mesh

@@ -181,11 +181,57 @@ namespace {
 
 void count_kernels(mesh_ctx *c, int stage, int n);
 
+// Copy stream, events and split-point buffers of the pipelined host path.
+int ensure_pipe(mesh_ctx *c) {
+    if (c->copy) return MESH_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming);
+    for (int g = 0; g < PIPE_MAX && e == cudaSuccess; g++) e = cudaEventCreateWithFlags(&c->ev_part[g], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = c->gat.ensure(GATHER_MAX * sizeof(int64_t));
+    if (e == cudaSuccess && !c->h_gat) e = cudaHostAlloc((void **)&c->h_gat, GATHER_MAX * sizeof(int64_t), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        // leave no half-made pipeline behind: the next call retries from scratch
+        if (c->copy) cudaStreamDestroy(c->copy);
+        c->copy = nullptr;
+        return cuda_fail(c, e, "pipeline stream");
+    }
+    return MESH_OK;
+}
+
+// Host volume upload in c->ngroups groups of z segments on the copy stream, each
+// group classified on the compute stream as soon as it has arrived: group g holds
+// the sample planes its segments read (segment s reads planes s*zs ..
+// min((s+1)*zs, cz)).  Copies and launches are enqueued alternately, so that a
+// pageable source (whose copies return only once staged) overlaps too.
+cudaError_t upload_and_classify(mesh_ctx *c) {
+    const Plan &P = c->plan;
+    const size_t plane = (size_t)P.nx * P.ny * dtype_size(P.T);
+    cudaError_t e = cudaEventRecord(c->ev_ready, c->stream);  // earlier work on the volume buffer
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy, c->ev_ready, 0);
+    int64_t p0 = 0;
+    int s0 = 0;
+    for (int g = 0; g < c->ngroups && e == cudaSuccess; g++) {
+        const int s1 = (int)((int64_t)(g + 1) * P.nseg / c->ngroups);
+        const int64_t p1 = g + 1 == c->ngroups ? P.nz : std::min<int64_t>((int64_t)s1 * P.zs, P.nz - 1) + 1;
+        if (p1 > p0)
+            e = cudaMemcpyAsync((char *)c->vol.ptr + p0 * plane, (const char *)c->upl_src + p0 * plane,
+                                (size_t)(p1 - p0) * plane, cudaMemcpyHostToDevice, c->copy);
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_part[g], c->copy);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_part[g], 0);
+        if (e == cudaSuccess && s1 > s0) e = launch_classify(P, c->stream, s0, s1 - s0);
+        p0 = std::max(p0, p1);
+        s0 = s1;
+    }
+    return e;
+}
+
 int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
             const mesh_params *p) {
     Plan &P = c->plan;
     P = Plan{};
     c->have_plan = 0;
+    c->ngroups = 1;
     P.nx = nx; P.ny = ny; P.nz = nz;
     P.cx = (int32_t)(nx - 1); P.cy = (int32_t)(ny - 1); P.cz = (int32_t)(nz - 1);
     set_types(P, T, p, &c->Q64, &c->A64, &c->P64);
@@ -225,9 +271,15 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     } else {
         cudaGetLastError();
         if ((e = c->vol.ensure(vbytes)) != cudaSuccess) return cuda_fail(c, e, "volume buffer");
-        if ((e = cudaMemcpyAsync(c->vol.ptr, vol, vbytes, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
-            return cuda_fail(c, e, "volume upload");
         P.vol = c->vol.ptr;
+        if (c->pipe_bytes > 0 && (int64_t)vbytes >= c->pipe_bytes && P.nseg >= 2 && !c->want_tma && !c->one_walk) {
+            int rc = ensure_pipe(c);
+            if (rc) return rc;
+            c->ngroups = std::min(PIPE_MAX, P.nseg);  // the count uploads and classifies
+            c->upl_src = vol;
+        } else if ((e = cudaMemcpyAsync(c->vol.ptr, vol, vbytes, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) {
+            return cuda_fail(c, e, "volume upload");
+        }
     }
 
     // coordinate tables: xp yp zp dx dy dz (double), the same as float, then the
@@ -349,11 +401,20 @@ int run_count(mesh_ctx *c) {
         return cuda_fail(c, e, "memset");
     c->use_tma = !one_walk(c) && make_tensor_map(c);
     mark(c, 0);
-    if (one_walk(c)) e = launch_walk_mc(P, c->stream);
-    else e = c->use_tma ? launch_classify_tma(P, c->tmap, c->stream) : launch_classify(P, c->stream);
+    int nlaunch = 1;
+    if (one_walk(c)) {
+        e = launch_walk_mc(P, c->stream);
+    } else if (c->use_tma) {
+        e = launch_classify_tma(P, c->tmap, c->stream);
+    } else if (c->ngroups > 1) {
+        e = upload_and_classify(c);
+        nlaunch = c->ngroups;
+    } else {
+        e = launch_classify(P, c->stream);
+    }
     if (e != cudaSuccess) return cuda_fail(c, e, "classify launch");
     mark(c, 0);
-    count_kernels(c, 0, 1);
+    count_kernels(c, 0, nlaunch);
     mark(c, 1);
     if ((e = launch_scan(P, c->stream)) != cudaSuccess) return cuda_fail(c, e, "scan launch");
     mark(c, 1);
@@ -428,6 +489,76 @@ int launch_emit(mesh_ctx *c) {
     return MESH_OK;
 }
 
+// Marching Cubes emission into host buffers in K x ranges of whole x tiles.  The
+// emission order is x-major, so the cells of an x range own one contiguous run of
+// list entries, vertices and faces, starting at the scanned base of the range's
+// first piece (seg 0, y 0, x0).  Range g is compacted and expanded on the compute
+// stream; its vertices and faces go down on the copy stream while range g + 1 is
+// emitted.  All launches are enqueued before the copies, so a pageable (blocking)
+// destination still overlaps the copies with the emission.
+int emit_pipelined(mesh_ctx *c, int K, void *verts, int64_t *faces) {
+    const Plan &P = c->plan;
+    const int64_t np = P.pstride;
+    const size_t vsz = (size_t)3 * (P.out64 ? 8 : 4);
+    int tx[PIPE_MAX + 1];
+    for (int g = 0; g <= K; g++) tx[g] = (int)((int64_t)g * P.tiles_x / K);
+    GatherIdx gi{};
+    gi.n = 3 * (K - 1);
+    for (int g = 1; g < K; g++) {
+        const int64_t i = piece(P, 0, 0, tx[g] * TILE_X);
+        for (int k = 0; k < 3; k++) gi.idx[3 * (g - 1) + k] = k * np + i;
+    }
+    cudaError_t e = launch_gather(P.base, gi, (int64_t *)c->gat.ptr, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->h_gat, c->gat.ptr, (size_t)gi.n * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "split points");
+    int64_t V[PIPE_MAX + 1], F[PIPE_MAX + 1], E[PIPE_MAX + 1];
+    V[0] = F[0] = E[0] = 0;
+    V[K] = c->nverts;
+    F[K] = c->nfaces;
+    E[K] = c->nactive;
+    for (int g = 1; g < K; g++) {
+        V[g] = c->h_gat[3 * (g - 1)];
+        F[g] = c->h_gat[3 * (g - 1) + 1];
+        E[g] = c->h_gat[3 * (g - 1) + 2];
+    }
+    for (int g = 0; g < K; g++)
+        if (V[g] > V[g + 1] || F[g] > F[g + 1] || E[g] > E[g + 1] || V[g + 1] > c->nverts || F[g + 1] > c->nfaces)
+            return fail(c, MESH_EDEVICE, "inconsistent split points");
+    int nexp = 0;
+    mark(c, 2);
+    for (int g = 0; g < K && e == cudaSuccess; g++) {
+        Plan q = P;
+        q.tx0 = tx[g];
+        q.ntx = tx[g + 1] - tx[g];
+        q.e_lo = E[g];
+        q.e_hi = E[g + 1];
+        e = launch_emit_mc(q, c->Q64, c->P64, 0, c->stream);
+        if (e == cudaSuccess && E[g + 1] > E[g]) {
+            e = launch_emit_mc(q, c->Q64, c->P64, 1, c->stream);
+            nexp++;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_part[g], c->stream);
+    }
+    mark(c, 2);
+    count_kernels(c, 2, K);
+    count_kernels(c, 3, nexp);
+    if (e != cudaSuccess) return cuda_fail(c, e, "emit launch");
+    for (int g = 0; g < K && e == cudaSuccess; g++) {
+        e = cudaStreamWaitEvent(c->copy, c->ev_part[g], 0);
+        if (e == cudaSuccess && V[g + 1] > V[g])
+            e = cudaMemcpyAsync((char *)verts + V[g] * vsz, (const char *)P.verts + V[g] * vsz,
+                                (size_t)(V[g + 1] - V[g]) * vsz, cudaMemcpyDeviceToHost, c->copy);
+        if (e == cudaSuccess && F[g + 1] > F[g])
+            e = cudaMemcpyAsync(faces + 3 * F[g], P.faces + 3 * F[g], (size_t)(F[g + 1] - F[g]) * 24,
+                                cudaMemcpyDeviceToHost, c->copy);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->copy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_done, 0);
+    return e != cudaSuccess ? cuda_fail(c, e, "mesh download") : MESH_OK;
+}
+
 // Staging slots of the one walk beyond its active cells: at most a block per warp.
 int64_t stage_slack(const Plan &P) { return (int64_t)STG_BLK * P.tiles_x * P.tiles_y * P.nseg; }
 
@@ -499,6 +630,8 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     c->one_walk = ow && ow[0] == '1';
     const char *zc = getenv("MESHING_GB300_ZEROCOPY");
     c->zerocopy = zc && zc[0] == '1';
+    const char *pb = getenv("MESHING_GB300_PIPELINE_BYTES");  // <= 0: never pipelined
+    if (pb && pb[0]) c->pipe_bytes = strtoll(pb, nullptr, 10);
     *out = c;
     return MESH_OK;
 }
@@ -507,9 +640,16 @@ void mesh_ctx_destroy(mesh_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->vol, &c->tabs, &c->cnt,   &c->base,  &c->flags,    &c->scan,  &c->misc,
-                      &c->out_v, &c->out_f, &c->ent, &c->nrm, &c->weld_buf, &c->weld_v};
+    if (c->copy) cudaStreamSynchronize(c->copy);
+    DevBuf *bufs[] = {&c->vol,   &c->tabs,  &c->cnt, &c->base, &c->flags,    &c->scan,   &c->misc,
+                      &c->out_v, &c->out_f, &c->ent, &c->nrm,  &c->weld_buf, &c->weld_v, &c->gat};
     for (DevBuf *b : bufs) b->release();
+    for (cudaEvent_t e : c->ev_part)
+        if (e) cudaEventDestroy(e);
+    if (c->ev_ready) cudaEventDestroy(c->ev_ready);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
+    if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->h_gat) cudaFreeHost(c->h_gat);
     for (auto &v : c->ev_pairs)
         for (cudaEvent_t e : v) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ev_free) cudaEventDestroy(e);
@@ -659,12 +799,23 @@ int mesh_fill(mesh_ctx *c, void *verts, int64_t *faces, int out_on_device) {
     int rc;
     if (P.alg == MESH_ALG_MC && !one_walk(c) && (rc = ensure_entries(c, c->nactive))) return rc;
     if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
-    if ((rc = launch_emit(c))) return rc;
-    if (!out_on_device) {
-        if (vb && (e = cudaMemcpyAsync(verts, P.verts, vb, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
-            return cuda_fail(c, e, "vertex download");
-        if (fbytes && (e = cudaMemcpyAsync(faces, P.faces, fbytes, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
-            return cuda_fail(c, e, "face download");
+    int parts = 1;
+    if (!out_on_device && P.alg == MESH_ALG_MC && !one_walk(c) && c->pipe_bytes > 0 &&
+        (int64_t)(vb + fbytes) >= c->pipe_bytes && P.tiles_x >= 2) {
+        if ((rc = ensure_pipe(c))) return rc;
+        parts = std::min(PIPE_MAX, P.tiles_x);
+    }
+    if (parts > 1) {
+        if ((rc = emit_pipelined(c, parts, verts, faces))) return rc;
+    } else {
+        if ((rc = launch_emit(c))) return rc;
+        if (!out_on_device) {
+            if (vb && (e = cudaMemcpyAsync(verts, P.verts, vb, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+                return cuda_fail(c, e, "vertex download");
+            if (fbytes &&
+                (e = cudaMemcpyAsync(faces, P.faces, fbytes, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+                return cuda_fail(c, e, "face download");
+        }
     }
     if ((rc = fetch_misc(c))) return rc;
     c->have_plan = 0;  // a plan may reference a caller's device volume: one fill per count

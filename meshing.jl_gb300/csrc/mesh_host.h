@@ -16,6 +16,8 @@ constexpr int NSTAGE = 4;  // classify (or the one-walk MC pass), scan, emit (se
 // device word slots of the misc buffer: totals[NCNT], error word, work counter,
 // staging counter
 constexpr int MISC_SLOTS = NCNT + 3;
+// parts of the pipelined host path: upload groups of z segments, x ranges of the emission
+constexpr int PIPE_MAX = 8;
 
 struct DevBuf {
     void *ptr = nullptr;
@@ -57,6 +59,21 @@ struct mesh_ctx {
     int weld = 0;
     mesh::DevBuf weld_buf, weld_v;
     int64_t *h_misc = nullptr;  // pinned: totals[NCNT], err
+    // Pipelined host path (MESHING_GB300_PIPELINE_BYTES, default 256 MiB: host
+    // volumes and meshes at least this large).  mesh_count uploads the volume in
+    // groups of z segments on the copy stream and classifies each group as soon
+    // as its planes have arrived; mesh_fill emits the Marching Cubes mesh in x
+    // ranges (contiguous in the x-major emission order) and downloads each range
+    // on the copy stream while the next one is emitted.  Events order the two
+    // streams; the split points come from the scanned piece bases (gat / h_gat).
+    int64_t pipe_bytes = (int64_t)256 << 20;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_ready = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_part[mesh::PIPE_MAX] = {};
+    int ngroups = 1;
+    const void *upl_src = nullptr;  // the host volume of the count in progress
+    mesh::DevBuf gat;
+    int64_t *h_gat = nullptr;
     mesh::Plan plan{};
     int have_plan = 0;
     int Q64 = 0, A64 = 0, P64 = 0;

@@ -112,6 +112,11 @@ struct Plan {
     int64_t nitems;
     int32_t nvols, nstiles;
     int32_t vol_outputs;  // 1: every volume writes to its own BatchVol::verts / faces
+    // sub-range launches of the pipelined host path (zero: the whole volume):
+    // classify z segments seg0 .. seg0 + gridDim.z - 1; compact the x tiles
+    // tx0 .. tx0 + ntx - 1; expand list entries e_lo .. e_hi - 1
+    int32_t seg0, tx0, ntx;
+    int64_t e_lo, e_hi;
 };
 
 // One volume of a batch.  Its work items, pieces, activity bytes and scan
@@ -217,7 +222,14 @@ cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s);
 cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s);
 cudaError_t launch_compact_batch(const Plan &p, int ctas, cudaStream_t s);
 cudaError_t launch_expand_batch(const Plan &p, int Q64, int P64, cudaStream_t s);
-cudaError_t launch_classify(const Plan &p, cudaStream_t s);
+cudaError_t launch_classify(const Plan &p, cudaStream_t s, int seg0 = 0, int nsegs = 0);  // nsegs 0: all
+// A few values of a device int64 array for the host: dst[i] = src[idx[i]], i < n.
+constexpr int GATHER_MAX = 32;
+struct GatherIdx {
+    int64_t idx[GATHER_MAX];
+    int n;
+};
+cudaError_t launch_gather(const int64_t *src, const GatherIdx &g, int64_t *dst, cudaStream_t s);
 cudaError_t launch_scan(const Plan &p, cudaStream_t s);
 cudaError_t launch_emit(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
 // Marching Cubes in one walk: classify + stage entries, then expand them.

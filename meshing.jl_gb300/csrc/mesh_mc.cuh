@@ -309,15 +309,23 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
         s_f[i] = MC_CASE_FACES[i];
     }
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int64_t na = STAGED ? (int64_t)min(*p.stage_next, (unsigned long long)p.ent_cap) : min(p.totals[2], p.ent_cap);
+    int64_t na = STAGED ? (int64_t)min(*p.stage_next, (unsigned long long)p.ent_cap) : min(p.totals[2], p.ent_cap);
+    // ordered sub-range e_lo .. e_hi - 1: the blocks that hold it, with the
+    // entries of those blocks before e_lo counted (offsets) but not emitted
+    int64_t e_lo = 0;
+    if (MODE == EXP_ORDERED) {
+        if (p.e_hi > 0) na = min(na, p.e_hi);
+        e_lo = p.e_lo;
+    }
     const int64_t nblocks = (na + XW - 1) / XW;
     const int64_t np = p.pstride;
     const uint64_t pmask = (1ull << POS_BITS) - 1;
     const Tabs tb = tabs_of(p);
     __syncthreads();
 
-    for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+    for (int64_t blk = e_lo / XW + blockIdx.x; blk < nblocks; blk += gridDim.x) {
         const int64_t e = blk * XW + tid;
+        const int skip = (int)max((int64_t)0, e_lo - blk * XW);  // entries of this block before e_lo
         int nv = 0, nf = 0;
         if (e < na) {
             const int cs = p.ent_cs[e];
@@ -392,6 +400,7 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
         __syncthreads();
         for (int t = tid; t < V; t += XW) {
             const int j = sm.vmap[t];
+            if (j < skip) continue;
             const int k = t - sm.vs[j];
             const uint64_t pos = sm.pos[j];
             const int ed = (int)((s_v[sm.cs[j]] >> (4 * k)) & 15u);
@@ -424,6 +433,7 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
         }
         for (int t = tid; t < F; t += XW) {
             const int j = sm.fmap[t];
+            if (j < skip) continue;
             const int k = t - sm.fs[j];
             const unsigned s = (unsigned)(s_f[sm.cs[j]] >> (12 * k));
             // 1-based within the volume
