@@ -408,14 +408,17 @@ __global__ void __launch_bounds__(256) k_classify(const Plan p) {
     __syncthreads();
     const int ty = blockIdx.y * WARPS + (threadIdx.x >> 5);
     if (ty * CWY >= p.cy) return;  // warp-uniform
-    const int seg = p.seg0 + (int)blockIdx.z;
+    // a launch over segments seg0 .. seg1 - 1 (seg1 0: all) spans the whole grid and
+    // its other blocks return at once: the segment stays the block index, which the
+    // walks re-read instead of keeping it live
+    if ((int)blockIdx.z < p.seg0 || (p.seg1 > 0 && (int)blockIdx.z >= p.seg1)) return;
     if (ALG == MESH_ALG_MC) {
-        if (tile_inner(p, blockIdx.x, ty, seg))
-            classify_tile_mc_inner<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, seg);
+        if (tile_inner(p, blockIdx.x, ty, blockIdx.z))
+            classify_tile_mc_inner<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
         else
-            classify_tile_mc<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, seg);
+            classify_tile_mc<T>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
     } else
-        classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, seg);
+        classify_tile<T, ALG>(p, s_tab, threadIdx.x & 31, blockIdx.x, ty, blockIdx.z);
 }
 
 // Batch (Marching Cubes): persistent warps take work items -- a warp tile of
@@ -597,9 +600,9 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
     if (tid == 0 && s_fail) atomicOr(p.err, ERR_TMA_TIMEOUT);
 }
 
-template <class T> cudaError_t launch_t(const Plan &p, cudaStream_t s, int nsegs) {
+template <class T> cudaError_t launch_t(const Plan &p, cudaStream_t s) {
     const int ty = (p.cy + CWY - 1) / CWY;  // warp tiles of the load walk along y
-    dim3 grid(p.tiles_x, (ty + WARPS - 1) / WARPS, nsegs);
+    dim3 grid(p.tiles_x, (ty + WARPS - 1) / WARPS, p.nseg);
     switch (p.alg) {
     case MESH_ALG_MC: k_classify<T, MESH_ALG_MC><<<grid, 32 * WARPS, 0, s>>>(p); break;
     case MESH_ALG_MT: k_classify<T, MESH_ALG_MT><<<grid, 32 * WARPS, 0, s>>>(p); break;
@@ -683,19 +686,20 @@ cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s) {
 // Segments seg0 .. seg0 + nsegs - 1 (nsegs 0: every segment).
 cudaError_t launch_classify(const Plan &p0, cudaStream_t s, int seg0, int nsegs) {
     Plan p = p0;
-    p.seg0 = seg0;
     if (nsegs <= 0) nsegs = p.nseg - seg0;
     if (seg0 < 0 || nsegs <= 0 || seg0 + nsegs > p.nseg) return cudaErrorInvalidValue;
+    p.seg0 = seg0;
+    p.seg1 = seg0 + nsegs;
     switch (p.T) {
-    case MESH_DT_U16: return launch_t<uint16_t>(p, s, nsegs);
-    case MESH_DT_F16: return launch_t<h16>(p, s, nsegs);
-    case MESH_DT_I16: return launch_t<int16_t>(p, s, nsegs);
-    case MESH_DT_I8: return launch_t<int8_t>(p, s, nsegs);
-    case MESH_DT_U8: return launch_t<uint8_t>(p, s, nsegs);
-    case MESH_DT_F32: return launch_t<float>(p, s, nsegs);
-    case MESH_DT_I32: return launch_t<int32_t>(p, s, nsegs);
-    case MESH_DT_I64: return launch_t<int64_t>(p, s, nsegs);
-    default: return launch_t<double>(p, s, nsegs);
+    case MESH_DT_U16: return launch_t<uint16_t>(p, s);
+    case MESH_DT_F16: return launch_t<h16>(p, s);
+    case MESH_DT_I16: return launch_t<int16_t>(p, s);
+    case MESH_DT_I8: return launch_t<int8_t>(p, s);
+    case MESH_DT_U8: return launch_t<uint8_t>(p, s);
+    case MESH_DT_F32: return launch_t<float>(p, s);
+    case MESH_DT_I32: return launch_t<int32_t>(p, s);
+    case MESH_DT_I64: return launch_t<int64_t>(p, s);
+    default: return launch_t<double>(p, s);
     }
 }
 

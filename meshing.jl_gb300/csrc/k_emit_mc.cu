@@ -265,7 +265,7 @@ template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cu
     static int grid_a = 0, grid_b = 0;  // per instantiation: resident CTAs on this device
     if (!grid_a) {
         grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
-        grid_b = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>, XW);
+        grid_b = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>);
     }
     if (stage == 0) {
         const int nitems = (p.ntx > 0 ? p.ntx : p.tiles_x) * ((p.cy + CR - 1) / CR) * p.nseg;
@@ -306,7 +306,7 @@ template <class T> cudaError_t compact_batch_t(const Plan &p, int ctas, cudaStre
 
 template <class T, class Q, class P> cudaError_t expand_batch_t(const Plan &p, cudaStream_t s) {
     static int grid = 0;  // per instantiation: resident CTAs on this device
-    if (!grid) grid = resident_ctas((const void *)k_expand_mc<T, Q, P, EXP_BATCH>, XW);
+    if (!grid) grid = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_BATCH>);
     k_expand_mc<T, Q, P, EXP_BATCH><<<grid, XW, 0, s>>>(p);
     return cudaGetLastError();
 }

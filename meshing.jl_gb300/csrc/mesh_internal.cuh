@@ -113,9 +113,9 @@ struct Plan {
     int32_t nvols, nstiles;
     int32_t vol_outputs;  // 1: every volume writes to its own BatchVol::verts / faces
     // sub-range launches of the pipelined host path (zero: the whole volume):
-    // classify z segments seg0 .. seg0 + gridDim.z - 1; compact the x tiles
-    // tx0 .. tx0 + ntx - 1; expand list entries e_lo .. e_hi - 1
-    int32_t seg0, tx0, ntx;
+    // classify z segments seg0 .. seg1 - 1; compact the x tiles tx0 .. tx0 + ntx - 1;
+    // expand list entries e_lo .. e_hi - 1
+    int32_t seg0, seg1, tx0, ntx;
     int64_t e_lo, e_hi;
 };
 

@@ -398,9 +398,10 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
             sm.fb[tid] = fb0 + fs;
         }
         __syncthreads();
-        for (int t = tid; t < V; t += XW) {
+        // the entries before e_lo come first in the block's numbering: start after them
+        const int v0 = skip ? sm.vs[skip] : 0, f0 = skip ? sm.fs[skip] : 0;
+        for (int t = v0 + tid; t < V; t += XW) {
             const int j = sm.vmap[t];
-            if (j < skip) continue;
             const int k = t - sm.vs[j];
             const uint64_t pos = sm.pos[j];
             const int ed = (int)((s_v[sm.cs[j]] >> (4 * k)) & 15u);
@@ -431,9 +432,8 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
                 p.vkey[out] = key | (own ? (long long)(1ull << 63) : 0ll);
             }
         }
-        for (int t = tid; t < F; t += XW) {
+        for (int t = f0 + tid; t < F; t += XW) {
             const int j = sm.fmap[t];
-            if (j < skip) continue;
             const int k = t - sm.fs[j];
             const unsigned s = (unsigned)(s_f[sm.cs[j]] >> (12 * k));
             // 1-based within the volume
@@ -465,6 +465,37 @@ inline int resident_ctas(const void *fn, int threads) {
         cudaGetLastError();
         per_sm = 1;
     }
+    return per_sm * sms;
+}
+
+
+// Shared memory the expansion keeps per SM (KB): its coordinate-table loads hit
+// in L1, which gets the rest of the SM's 256 KB.  164 KB hold 6 CTAs (26 KB each
+// for Float32 volumes) and leave 92 KB of L1.  1024^3 Float32 sines field:
+// 164 KB 0.736 ms, 228 KB (8 CTAs) 0.760, 132 KB (4 CTAs) 0.822, 100 KB 0.951.
+#ifndef EXPAND_SMEM_KB
+#define EXPAND_SMEM_KB 164
+#endif
+
+// Resident CTAs of an expansion kernel with its shared-memory carveout set to
+// EXPAND_SMEM_KB: the occupancy calculator's figure, clamped to what the carveout holds.
+inline int expand_ctas(const void *fn) {
+    int dev = 0, sms = 0, smem_sm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const int want = EXPAND_SMEM_KB * 1024;
+    if (smem_sm > 0 && want < smem_sm)  // percent of the maximum, rounded down to stay at or under it
+        cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)((int64_t)want * 100 / smem_sm));
+    cudaGetLastError();
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, XW, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && fa.sharedSizeBytes > 0)
+        per_sm = std::max(1, std::min(per_sm, (int)(std::min(want, smem_sm) / (int)(fa.sharedSizeBytes + 1024))));
+    cudaGetLastError();
     return per_sm * sms;
 }
 
