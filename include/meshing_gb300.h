@@ -95,7 +95,12 @@ typedef struct mesh_ctx mesh_ctx;
 /* Creates a context bound to CUDA device `device` with its own stream. */
 MESH_API int mesh_ctx_create(int device, mesh_ctx **out);
 MESH_API void mesh_ctx_destroy(mesh_ctx *ctx);
-/* Makes the context issue its work on `stream` (a cudaStream_t; NULL = the context's own). */
+/* Makes the context issue its work on `stream` (a cudaStream_t; NULL = the context's own).
+   Host-buffer calls on volumes or meshes of at least MESHING_GB300_PIPELINE_BYTES (default
+   256 MiB; 0 = never) also use a second, internal copy stream, ordered against `stream` by
+   events: mesh_count uploads in groups of z segments, each classified on arrival, and
+   mesh_fill downloads a Marching Cubes mesh in x ranges while the next range is emitted.
+   Both calls still return only when their work is complete. */
 MESH_API int mesh_ctx_set_stream(mesh_ctx *ctx, void *stream);
 /* No counterpart in the reference.  Until reset with (0, 0), the volumes of the
  * context's calls are x samples x_first .. x_first+nx-1 of a volume whose x axis

@@ -192,6 +192,10 @@ int ensure_pipe(mesh_ctx *c) {
     if (e == cudaSuccess && !c->h_gat) e = cudaHostAlloc((void **)&c->h_gat, GATHER_MAX * sizeof(int64_t), cudaHostAllocDefault);
     if (e != cudaSuccess) {
         // leave no half-made pipeline behind: the next call retries from scratch
+        for (cudaEvent_t &ev : c->ev_part)
+            if (ev) cudaEventDestroy(ev), ev = nullptr;
+        if (c->ev_ready) cudaEventDestroy(c->ev_ready), c->ev_ready = nullptr;
+        if (c->ev_done) cudaEventDestroy(c->ev_done), c->ev_done = nullptr;
         if (c->copy) cudaStreamDestroy(c->copy);
         c->copy = nullptr;
         return cuda_fail(c, e, "pipeline stream");
