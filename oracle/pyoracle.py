@@ -130,6 +130,9 @@ def isosurface(vol, alg='mc', iso=0.0, eps=1e-3, ranges=((-1, 1), (-1, 1), (-1, 
     nx, ny, nz = vol.shape
     T = vol.dtype.type
     R = _jl_type(ranges[0][0])
+    weld = alg == 'mcw'  # welded Marching Cubes: one vertex per crossed lattice edge, first touch wins
+    if weld:
+        alg = 'mc'
     tys = [R, T, _jl_type(iso)] + ([_jl_type(eps)] if alg == 'mt' else [])
     FT = _promote(*tys)
     O = _float(FT) if FT not in _INTS else np.float64
@@ -146,6 +149,7 @@ def isosurface(vol, alg='mc', iso=0.0, eps=1e-3, ranges=((-1, 1), (-1, 1), (-1, 
 
     if alg == 'mc':
         corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+        welded = {}  # (lower lattice node, axis) -> 1-based welded vertex
         for xi in range(nx - 1):
             for yi in range(ny - 1):
                 for zi in range(nz - 1):
@@ -154,19 +158,29 @@ def isosurface(vol, alg='mc', iso=0.0, eps=1e-3, ranges=((-1, 1), (-1, 1), (-1, 
                     if ci in (0, 255):
                         continue
                     p = [(xp[xi + a], yp[yi + b], zp[zi + c]) for a, b, c in corner]
-                    fct = len(verts)
+                    ids = []  # 1-based output index of the cell's k-th vertex
                     for vt in _T['R_MC_VERTS'][ci - 1]:
                         if vt == 0:
                             break
                         a, b = (int(e) - 1 for e in _T['R_MC_EDGE_LIST'][vt - 1])
+                        if weld:
+                            na = (xi + corner[a][0], yi + corner[a][1], zi + corner[a][2])
+                            nb = (xi + corner[b][0], yi + corner[b][1], zi + corner[b][2])
+                            key = (min(na, nb), [na[k] != nb[k] for k in range(3)].index(True))
+                            if key in welded:
+                                ids.append(welded[key])
+                                continue
                         mu = _quot(iso, v[a], v[b])
                         verts.append(tuple(O(_add(p[a][k], _mul(mu, p[b][k] - p[a][k]))) for k in range(3)))
+                        ids.append(len(verts))
+                        if weld:
+                            welded[key] = len(verts)
                     o = _T['R_MC_CONNECTIVITY'][_T['R_MC_EQ_MAPPING'][ci - 1] - 1]
-                    faces.append((fct + 3, fct + 2, fct + 1))
+                    faces.append((ids[2], ids[1], ids[0]))
                     for i in (0, 3, 6, 9):
                         if o[i] == 0:
                             break
-                        faces.append((fct + int(o[i + 2]), fct + int(o[i + 1]), fct + int(o[i])))
+                        faces.append((ids[int(o[i + 2]) - 1], ids[int(o[i + 1]) - 1], ids[int(o[i]) - 1]))
     elif alg == 'mt':
         corner = [(0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1)]
         ids = {}

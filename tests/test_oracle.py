@@ -274,3 +274,25 @@ def test_welded_mc_is_the_deduplicated_mesh(oracle, dt, iso):
         used = np.unique(wf)
         assert len(used) == len(wv)
         assert set(np.arange(1, len(wv) + 1)) == set(used.tolist())
+
+
+def test_welded_mc_c_matches_python_restatement(oracle):
+    # the welded mode restated twice: oracle.c (run_mc_welded) and pyoracle.py (a dict of
+    # lattice edges over the plain Marching Cubes loop); positions from the first cell
+    # that meets an edge, so UInt16 wraparound and Float16 rounding carry through unchanged
+    rng = np.random.default_rng(5)
+    cases = [(np.float64, 0.0), (np.float32, np.float32(0.1)), (np.float32, 0.0), (np.uint16, 500),
+             (np.uint16, 250.25), (np.int16, 3), (np.float16, np.float32(0.0))]
+    for trial in range(4):
+        sh = tuple(int(x) for x in rng.integers(2, 8, 3))
+        for dt, iso in cases:
+            if dt in (np.uint16, np.int16):
+                A = rng.integers(0, 1000, sh).astype(dt)
+            else:
+                A = rng.standard_normal(sh).astype(dt)
+            A = np.asfortranarray(A)
+            a = oracle.isosurface(A, 'mcw', iso)
+            b = pyoracle.isosurface(A, 'mcw', iso)
+            assert a[0].dtype == b[0].dtype
+            assert np.array_equal(a[1], b[1]), (dt, sh)
+            assert np.array_equal(a[0], b[0], equal_nan=True), (dt, sh)
