@@ -234,6 +234,61 @@ def isosurface(vol, alg='mc', iso=0.0, eps=1e-3, ranges=((-1, 1), (-1, 1), (-1, 
                             continue
                         f = [vid(ve(e[3])), vid(ve(e[4])), vid(ve(e[5]))]
                         faces.append(tuple(f))
+    elif alg == 'nsn':
+        # NaiveSurfaceNets as this project defines it (the reference has none): one vertex
+        # per active cell at the mean of its Marching Cubes edge crossings (summed from 0
+        # in P, divided in Float64 and rounded to P, then to the output type); one quad per
+        # crossed lattice edge with four cells around it, split into two triangles
+        # oriented by which end of the edge lies below iso
+        corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+        cid = {}
+        for xi in range(nx - 1):
+            for yi in range(ny - 1):
+                for zi in range(nz - 1):
+                    v = [vol[xi + a, yi + b, zi + c] for a, b, c in corner]
+                    ci = sum(1 << k for k in range(8) if below(v[k]))
+                    if ci in (0, 255):
+                        continue
+                    p = [(xp[xi + a], yp[yi + b], zp[zi + c]) for a, b, c in corner]
+                    acc, n = None, 0
+                    for e in range(12):
+                        a, b = (int(t) - 1 for t in _T['R_MC_EDGE_LIST'][e])
+                        if ((ci >> a) & 1) == ((ci >> b) & 1):
+                            continue
+                        mu = _quot(iso, v[a], v[b])
+                        x = [_add(p[a][k], _mul(mu, p[b][k] - p[a][k])) for k in range(3)]
+                        if acc is None:
+                            acc = [type(x[k])(0) for k in range(3)]
+                        acc = [_add(acc[k], x[k]) for k in range(3)]
+                        n += 1
+                    Pt = type(acc[0])
+                    verts.append(tuple(O(Pt(np.float64(acc[k]) / np.float64(n))) for k in range(3)))
+                    cid[(xi, yi, zi)] = len(verts)
+        for xi in range(nx - 1):
+            for yi in range(ny - 1):
+                for zi in range(nz - 1):
+                    if (xi, yi, zi) not in cid:
+                        continue
+                    cc = (xi, yi, zi)
+                    s0 = below(vol[xi, yi, zi])
+                    for k in range(3):
+                        u, w = (k + 1) % 3, (k + 2) % 3
+                        if cc[u] == 0 or cc[w] == 0:
+                            continue
+                        n1 = list(cc)
+                        n1[k] += 1
+                        if below(vol[n1[0], n1[1], n1[2]]) == s0:
+                            continue
+                        a, b, d = list(cc), list(cc), list(cc)
+                        a[u] -= 1
+                        a[w] -= 1
+                        b[w] -= 1
+                        d[u] -= 1
+                        A, B, C, D = cid[tuple(a)], cid[tuple(b)], cid[cc], cid[tuple(d)]
+                        if s0:
+                            faces += [(A, B, C), (A, C, D)]
+                        else:
+                            faces += [(A, C, B), (A, D, C)]
     else:
         raise ValueError(alg)
     V = np.array(verts, dtype=O).reshape(-1, 3)

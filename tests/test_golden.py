@@ -58,7 +58,8 @@ def test_oracle_reproduces_golden(oracle, case):
 
 
 @pytest.mark.parametrize('name', ['single_cell_f32_mc', 'nonfinite_f64_mc', 'random_u16_mt_f64iso',
-                                  'flat_f64_mc', 'constant_f64_mt', 'sphere_f64_mcw', 'random_i64_mcw'])
+                                  'flat_f64_mc', 'constant_f64_mt', 'sphere_f64_mcw', 'random_i64_mcw',
+                                  'sphere_f64_nsn', 'random_i8_nsn', 'gyroid_f32_nsn_f32range'])
 def test_python_restatement_reproduces_golden(name):
     m, vol, v, f, iso, eps, ranges = CASES[IDS.index(name)]
     with np.errstate(all='ignore'):  # Inf - Inf in the non-finite case, as in the reference

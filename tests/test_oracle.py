@@ -296,3 +296,25 @@ def test_welded_mc_c_matches_python_restatement(oracle):
             assert a[0].dtype == b[0].dtype
             assert np.array_equal(a[1], b[1]), (dt, sh)
             assert np.array_equal(a[0], b[0], equal_nan=True), (dt, sh)
+
+
+def test_nsn_c_matches_python_restatement(oracle):
+    # NaiveSurfaceNets (defined by this project; the reference has none) restated twice:
+    # oracle.c (run_nsn) and pyoracle.py, over every scalar-type path and range type
+    rng = np.random.default_rng(9)
+    cases = [(np.float64, 0.0), (np.float32, np.float32(0.1)), (np.float32, 0.0), (np.uint16, 500),
+             (np.uint16, 250.25), (np.int16, 3), (np.float16, np.float32(0.0)), (np.int32, 7)]
+    for trial in range(3):
+        sh = tuple(int(x) for x in rng.integers(2, 8, 3))
+        for dt, iso in cases:
+            if dt in (np.uint16, np.int16, np.int32):
+                A = rng.integers(0, 1000, sh).astype(dt)
+            else:
+                A = rng.standard_normal(sh).astype(dt)
+            A = np.asfortranarray(A)
+            for rg in (((-1, 1),) * 3, ((np.float32(-2), np.float32(3)),) * 3, ((0.0, 1.5),) * 3):
+                a = oracle.isosurface(A, 'nsn', iso, 1e-3, rg)
+                b = pyoracle.isosurface(A, 'nsn', iso, 1e-3, rg)
+                assert a[0].dtype == b[0].dtype
+                assert np.array_equal(a[1], b[1]), (dt, sh, rg)
+                assert np.array_equal(a[0], b[0], equal_nan=True), (dt, sh, rg)
