@@ -128,6 +128,23 @@ def measured_peak():
         return 6800.0, 'fallback'
 
 
+def max_over_ranks(dist, values, device='cpu'):
+    """Each value's maximum over the ranks: the slowest replica sets the job's time
+    (identity without a process group)."""
+    if not dist:
+        return list(values)
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(units_per_rank, world, ms):
+    """Units per second of the whole job: every replica processes units_per_rank in
+    the slowest replica's ms."""
+    return units_per_rank * world / (ms * 1e-3)
+
+
 def _spread(xs):
     """min / median / p90 / max / mean of a list of step times (ms)."""
     if not xs:
@@ -285,10 +302,7 @@ def run_ours(args, rank, world, dist):
     ok = torch.equal(hv.to(dev), verts) and torch.equal(hf.to(dev), faces)
     link = host_link(hvol, hv, hf, dev)  # overwrites hv / hf: after the check
 
-    if dist:
-        t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = t.tolist()
+    ms, e2e_ms = max_over_ranks(dist, [ms, e2e_ms], dev)
     if rank != 0:
         return
     vox = float(n) ** 3
@@ -331,7 +345,7 @@ def run_ours(args, rank, world, dist):
                          'single-threaded like Meshing.jl), %.2f s' % (n, n, planes + 1, cdt)}
     line = {
         'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes',
-        'value': vox * world / (ms * 1e-3) / 1e9,
+        'value': whole_job_rate(vox, world, ms) / 1e9,
         'unit': 'Gvoxels/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
         'config': {'workload': WORKLOAD % n, 'nx': n, 'ny': n, 'nz': n, 'cells': (n - 1) ** 3, 'nverts': nv,
@@ -343,7 +357,7 @@ def run_ours(args, rank, world, dist):
                      'algorithmic_bytes': kern[dom]['bytes']},
         'kernels': kern,
         'pipeline': {'bytes': in_b + out_b, 'achieved': pipe_gbs, 'frac': pipe_gbs / peak, 'unit': 'GB/s'},
-        'e2e': {'value': vox * world / (e2e_ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': e2e_ms,
+        'e2e': {'value': whole_job_rate(vox, world, e2e_ms) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': e2e_ms,
                 'h2d_bytes_per_step': int(in_b), 'd2h_bytes_per_step': int(out_b),
                 'count_ms': _spread([c for c, _ in split]), 'fill_ms': _spread([f for _, f in split]),
                 'link': link, 'link_bound_ms': (in_b / link['h2d_gbs'] + out_b / link['d2h_gbs']) / 1e6},
