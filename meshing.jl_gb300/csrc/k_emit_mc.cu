@@ -262,11 +262,9 @@ __global__ void __launch_bounds__(256, COMPACT_MIN_CTAS) k_compact_batch(const P
 }
 
 template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cudaStream_t s) {
-    static int grid_a = 0, grid_b = 0;  // per instantiation: resident CTAs on this device
-    if (!grid_a) {
-        grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
-        grid_b = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>);
-    }
+    // per instantiation: resident CTAs on this device (thread-safe one-time initialisation)
+    static const int grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
+    static const int grid_b = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>);
     if (stage == 0) {
         const int nitems = (p.ntx > 0 ? p.ntx : p.tiles_x) * ((p.cy + CR - 1) / CR) * p.nseg;
         cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
@@ -305,8 +303,8 @@ template <class T> cudaError_t compact_batch_t(const Plan &p, int ctas, cudaStre
 }
 
 template <class T, class Q, class P> cudaError_t expand_batch_t(const Plan &p, cudaStream_t s) {
-    static int grid = 0;  // per instantiation: resident CTAs on this device
-    if (!grid) grid = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_BATCH>);
+    // per instantiation: resident CTAs on this device (thread-safe one-time initialisation)
+    static const int grid = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_BATCH>);
     k_expand_mc<T, Q, P, EXP_BATCH><<<grid, XW, 0, s>>>(p);
     return cudaGetLastError();
 }

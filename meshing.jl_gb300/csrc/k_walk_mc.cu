@@ -193,8 +193,8 @@ template <class T> cudaError_t walk_t(const Plan &p, cudaStream_t s) {
 }
 
 template <class T, class Q, class P> cudaError_t expand_t(const Plan &p, cudaStream_t s) {
-    static int grid = 0;  // per instantiation: resident CTAs on this device
-    if (!grid) grid = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_STAGED>);
+    // per instantiation: resident CTAs on this device (thread-safe one-time initialisation)
+    static const int grid = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_STAGED>);
     k_expand_mc<T, Q, P, EXP_STAGED><<<grid, XW, 0, s>>>(p);
     return cudaGetLastError();
 }

@@ -350,18 +350,16 @@ void mark(mesh_ctx *c, int stage) {
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    // thread-safe one-time lookup
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         cudaDriverEntryPointQueryResult q;
         void *f = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+        const bool ok = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                                         &q) == cudaSuccess &&
+                        q == cudaDriverEntryPointSuccess;
         cudaGetLastError();
-    }
+        return ok ? (PFN_cuTensorMapEncodeTiled_v12000)f : nullptr;
+    }();
     return fn;
 }
 
