@@ -318,3 +318,20 @@ def test_nsn_c_matches_python_restatement(oracle):
                 assert a[0].dtype == b[0].dtype
                 assert np.array_equal(a[1], b[1]), (dt, sh, rg)
                 assert np.array_equal(a[0], b[0], equal_nan=True), (dt, sh, rg)
+
+
+@pytest.mark.parametrize('n,r', [(48, 0.55), (33, 0.7), (64, 0.4)])
+def test_welded_mc_sphere_is_a_closed_sphere(oracle, n, r):
+    # welding turns the per-cell Marching Cubes triangles of a sphere into one closed,
+    # consistently oriented surface: every directed edge once with its reverse once,
+    # Euler characteristic 2, and it encloses the sphere's volume (within 1%)
+    v, f = oracle.isosurface(_sphere(n, r), 'mcw')
+    e = _edges(f)
+    key = e[:, 0] * (len(v) + 1) + e[:, 1]
+    rkey = e[:, 1] * (len(v) + 1) + e[:, 0]
+    assert len(np.unique(key)) == len(key)
+    assert np.array_equal(np.sort(key), np.sort(rkey))
+    assert len(v) - len(key) // 2 + len(f) == 2
+    p = v[f - 1]
+    vol = np.einsum('ij,ij->i', p[:, 0], np.cross(p[:, 1], p[:, 2])).sum() / 6
+    assert abs(vol / (4 / 3 * np.pi * r ** 3) - 1) < 0.01
