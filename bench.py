@@ -128,6 +128,18 @@ def measured_peak():
         return 6800.0, 'fallback'
 
 
+def pieces(nx, ny, nz, sms):
+    """Pieces (one z segment of one cell column) of a volume: the engine's tiling rule
+    (mesh_api.cu, prepare): 31 x 4-cell warp tiles, z segments of whole 8-cell chunks,
+    about 64 warp tiles per SM in all."""
+    cx, cy, cz = nx - 1, ny - 1, nz - 1
+    per_seg = ((cx + 30) // 31) * ((cy + 3) // 4)
+    nseg = min((cz + 7) // 8, max(1, (sms * 64 + per_seg - 1) // per_seg))
+    zs = (cz + nseg - 1) // nseg
+    zs = (zs + 7) // 8 * 8
+    return ((cz + zs - 1) // zs) * cy * cx
+
+
 def max_over_ranks(dist, values, device='cpu'):
     """Each value's maximum over the ranks: the slowest replica sets the job's time
     (identity without a process group)."""
@@ -316,9 +328,10 @@ def run_ours(args, rank, world, dist):
     # expand (k_expand_mc) writes the mesh; the scan reads 3 u32 counts and writes
     # 3 int64 bases per piece.  The active-cell list between compaction and
     # expansion is not counted.
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     kern = {
         'classify': {'ms': stage['classify'], 'bytes': in_b, 'kernel': 'k_classify'},
-        'scan': {'ms': stage['scan'], 'bytes': float((n - 1) ** 2 * 3 * (4 + 8)), 'kernel': 'k_scan'},
+        'scan': {'ms': stage['scan'], 'bytes': float(pieces(n, n, n, sms) * 3 * (4 + 8)), 'kernel': 'k_scan'},
         'compact': {'ms': stage['emit'], 'bytes': in_b, 'kernel': 'k_compact_mc'},
         'expand': {'ms': stage['expand'], 'bytes': float(out_b), 'kernel': 'k_expand_mc'},
     }
