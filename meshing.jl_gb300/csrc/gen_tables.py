@@ -272,7 +272,9 @@ def emit(out, mc, mt_t, mt):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    if len(sys.argv) != 2:
+        sys.exit('usage: %s <Meshing.jl checkout>' % sys.argv[0])
+    ref = sys.argv[1]
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'mesh_tables.h')
     verts, eqmap, conn, elist, tri = load_mc(ref)
     # edge list restated in the kernels must match the reference's (_mc_edge_list)

@@ -41,7 +41,9 @@ def c_array(name, ctype, data):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    if len(sys.argv) != 2:
+        sys.exit('usage: %s <Meshing.jl checkout>' % sys.argv[0])
+    ref = sys.argv[1]
     mc = open(os.path.join(ref, 'src/lut/mc.jl')).read()
     mt = open(os.path.join(ref, 'src/lut/mt.jl')).read()
     out = ['// Generated by gen_ref_luts.py from Meshing.jl v0.7.0 src/lut/mc.jl and src/lut/mt.jl.',

@@ -63,7 +63,9 @@ typedef struct {
     double hi_a;      /* one(T) - eps, in promote(T, E), promoted to A */
     const void *vol;
     int64_t nx, ny, nz;
+    int64_t sx;       /* samples per row in memory (nx, or the whole volume's nx for an x window) */
     double *xp, *yp, *zp;
+    double *xp_alloc; /* what linrange returned for x (xp is offset into it for an x window) */
 } orc_ctx;
 
 static double rnd(int ty, double x) { return ty == ORC_F32 ? (double)(float)x : x; }
@@ -108,7 +110,7 @@ static double half_value(uint16_t h) {
 static double round_half(double x) { return (double)(_Float16)x; }
 
 static double load(const orc_ctx *c, int64_t x, int64_t y, int64_t z) {
-    int64_t i = x + c->nx * (y + c->ny * z);
+    int64_t i = x + c->sx * (y + c->ny * z);
     switch (c->T) {
     case ORC_U16: return (double)((const uint16_t *)c->vol)[i];
     case ORC_U8: return (double)((const uint8_t *)c->vol)[i];
@@ -548,7 +550,7 @@ static int setup(orc_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int
     if (alg == ORC_MT && E != ORC_F32 && E != ORC_F64) return ORC_EINVAL;
     if (nx < 0 || ny < 0 || nz < 0) return ORC_EINVAL;
     c->T = T; c->I = I; c->E = E; c->R = R;
-    c->vol = vol; c->nx = nx; c->ny = ny; c->nz = nz;
+    c->vol = vol; c->nx = nx; c->ny = ny; c->nz = nz; c->sx = nx;
     c->iso = iso;
     /* promote(typeof(iso), T) for the quotient; Int / Int divides in Float64 */
     int q64 = (T == ORC_F64) || (I == ORC_F64) || (T != ORC_F32 && I == ORC_I64);
@@ -568,7 +570,7 @@ static int setup(orc_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int
         c->O = out_type(tys, 3);
     }
     (void)is_float;
-    c->xp = linrange(c->L, rg[0], rg[1], nx);
+    c->xp = c->xp_alloc = linrange(c->L, rg[0], rg[1], nx);
     c->yp = linrange(c->L, rg[2], rg[3], ny);
     c->zp = linrange(c->L, rg[4], rg[5], nz);
     if (!c->xp || !c->yp || !c->zp) return ORC_ENOMEM;
@@ -593,7 +595,31 @@ int orc_isosurface(const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, i
         else if (alg == ORC_NSN) rc = run_nsn(&c, out);
         else rc = ORC_EINVAL;
     }
-    free(c.xp); free(c.yp); free(c.zp);
+    free(c.xp_alloc); free(c.yp); free(c.zp);
+    return rc;
+}
+
+/* MarchingCubes over the x window of cells x0 .. x1 - 1 (samples x0 .. x1) of a
+ * volume of nx samples per row, with the whole volume's LinRange node
+ * coordinates.  The reference's loop is x-outermost (src/marching_cubes.jl:40),
+ * so the window's mesh is the contiguous block of the whole mesh that follows
+ * the vertices and faces of cells x < x0; its faces are numbered from 1 within
+ * the window.  Windows of one volume can run on several threads at once. */
+int orc_isosurface_mc_xwin(const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int64_t x0, int64_t x1, int I,
+                           double iso, int R, const double *range6, orc_mesh *out) {
+    orc_ctx c;
+    memset(out, 0, sizeof(*out));
+    if (x0 < 0 || x1 < x0 || x1 >= nx) return ORC_EINVAL;
+    int rc = setup(&c, vol, T, nx, ny, nz, ORC_MC, I, iso, ORC_F64, 1e-3, R, range6);
+    if (!rc) {
+        static const int size_of[10] = {0, 2, 4, 8, 8, 4, 2, 2, 1, 1};
+        c.vol = (const char *)vol + x0 * size_of[T];
+        c.xp = c.xp_alloc + x0;
+        c.nx = x1 - x0 + 1;
+        out->out_bits = c.O == ORC_F32 ? 32 : 64;
+        rc = run_mc(&c, out);
+    }
+    free(c.xp_alloc); free(c.yp); free(c.zp);
     return rc;
 }
 

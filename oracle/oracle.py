@@ -55,6 +55,11 @@ def lib():
                                         ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_Mesh)]
         _lib.orc_isosurface.restype = ctypes.c_int
+        _lib.orc_isosurface_mc_xwin.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
+                                                ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                                ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(_Mesh)]
+        _lib.orc_isosurface_mc_xwin.restype = ctypes.c_int
         _lib.orc_free.argtypes = [ctypes.POINTER(_Mesh)]
         _lib.orc_output_bits.argtypes = [ctypes.c_int] * 5
         _lib.orc_cubeindex.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_double]
@@ -100,6 +105,49 @@ def isosurface(vol, alg='mc', iso=0.0, eps=1e-3, ranges=((-1, 1), (-1, 1), (-1, 
                               scalar_type(eps), float(eps), R, rg, ctypes.byref(m))
     if rc:
         raise RuntimeError('oracle failed with status %d' % rc)
+    return _take(m)
+
+
+def _range_args(ranges):
+    rt = {scalar_type(ranges[a][b]) for a in range(3) for b in range(2)}
+    if len(rt) != 1:
+        raise TypeError('all range endpoints must share one type')
+    return rt.pop(), (ctypes.c_double * 6)(*[float(ranges[a][b]) for a in range(3) for b in range(2)])
+
+
+def mc_xwindow(vol, x0, x1, iso=0.0, ranges=((-1, 1), (-1, 1), (-1, 1))):
+    """MarchingCubes over the cells x0 .. x1-1 of ``vol`` (Fortran-ordered),
+    with the whole volume's LinRange node coordinates.  Returns the block of the
+    whole mesh that those cells emit, faces numbered from 1 within the block."""
+    if not vol.flags['F_CONTIGUOUS']:
+        raise ValueError('vol must be Fortran-ordered')
+    nx, ny, nz = vol.shape
+    R, rg = _range_args(ranges)
+    m = _Mesh()
+    rc = lib().orc_isosurface_mc_xwin(vol.ctypes.data, DTYPES[vol.dtype], nx, ny, nz, x0, x1, scalar_type(iso),
+                                      float(iso), R, rg, ctypes.byref(m))
+    if rc:
+        raise RuntimeError('oracle failed with status %d' % rc)
+    return _take(m)
+
+
+def mc_xwindows(vol, iso=0.0, ranges=((-1, 1), (-1, 1), (-1, 1)), windows=64, threads=None):
+    """The whole MarchingCubes mesh of ``vol`` as consecutive x-window blocks,
+    meshed on several threads (the C oracle runs without the GIL).  Returns a
+    list of (x0, x1, verts, faces) in emission order."""
+    from concurrent.futures import ThreadPoolExecutor
+    vol = np.asfortranarray(vol)
+    cx = vol.shape[0] - 1
+    cuts = sorted({round(i * cx / windows) for i in range(windows + 1)})
+    spans = list(zip(cuts[:-1], cuts[1:]))
+    threads = threads or max(1, min(len(spans), os.cpu_count() or 1))
+    with ThreadPoolExecutor(threads) as ex:
+        meshes = list(ex.map(lambda s: mc_xwindow(vol, s[0], s[1], iso, ranges), spans))
+    return [(a, b, v, f) for (a, b), (v, f) in zip(spans, meshes)]
+
+
+def _take(m):
+    """numpy copies of an orc_mesh's arrays; frees the mesh."""
     try:
         ft = np.float32 if m.out_bits == 32 else np.float64
         if m.nverts:

@@ -1,14 +1,14 @@
 """Full-size checks on the benchmark volume (1024^3 Float32 sines) and the
-512^3 UInt16 CT-like volume: properties that do not need the oracle to mesh
-the whole volume.
+512^3 UInt16 CT-like volume.
 
-* counts equal sum over cells of the per-case vertex / face counts, computed
-  here independently with torch from the oracle's reference-layout tables;
-* faces index existing vertices;
-* an x slab of cells is a contiguous block of the full output (emission order
-  is x-major), so it is compared with the oracle run on that slab:
-  connectivity exactly, positions to 2 ulp (the slab's own LinRange nodes can
-  differ from the full grid's by rounding);
+* the whole mesh is compared with the oracle bit for bit: the oracle meshes
+  consecutive x windows of cells with the whole volume's LinRange nodes on
+  all host cores (the reference's loop is x-outermost, src/marching_cubes.jl:40,
+  so each window's mesh is one contiguous block of the whole mesh), and every
+  vertex (as bits) and every face of the GPU mesh is checked against it;
+* counts also equal the sum over cells of the per-case vertex / face counts,
+  computed here independently with torch from the oracle's reference-layout
+  tables;
 * the exact float fast path for Float64 positions gives bit-identical output
   to the pure FP64 evaluation.
 """
@@ -65,7 +65,22 @@ def run_device(torch, pkg, t, method, ranges, ctx=None):
     return v, f
 
 
-def test_sines1024_counts_faces_and_slab(pkg, oracle, cuda, sines1024):
+def assert_whole_mesh(v, f, windows):
+    """GPU mesh (host numpy) == the oracle's x-window blocks, bit for bit."""
+    ibits = np.uint32 if v.dtype == np.float32 else np.uint64
+    vb = v.view(ibits)
+    vo = fo = 0
+    for x0, x1, ov, of in windows:
+        nv, nf = len(ov), len(of)
+        assert ov.dtype == v.dtype, (x0, x1)
+        assert np.array_equal(vb[vo:vo + nv], ov.view(ibits)), ('vertices differ in cells x0..x1-1', x0, x1)
+        assert np.array_equal(f[fo:fo + nf] - vo, of), ('faces differ in cells x0..x1-1', x0, x1)
+        vo += nv
+        fo += nf
+    assert (vo, fo) == (len(v), len(f))
+
+
+def test_sines1024_whole_mesh_bit_exact(pkg, oracle, cuda, sines1024):
     torch = cuda
     t = sines1024
     m = pkg.MarchingCubes(iso=np.float32(0))
@@ -73,23 +88,10 @@ def test_sines1024_counts_faces_and_slab(pkg, oracle, cuda, sines1024):
     assert v.dtype == torch.float32 and f.dtype == torch.int64
     cv, cf = torch_counts(torch, t, lambda s: s < 0)
     assert (v.shape[0], f.shape[0]) == (cv, cf)
-    assert int(f.min()) >= 1 and int(f.max()) == v.shape[0]
-    assert bool(torch.isfinite(v).all())
-    # x slab [x0, x1): its vertices start after those of cells x < x0
-    x0, x1 = 500, 524
-    before_v, before_f = torch_counts(torch, t[:x0 + 1], lambda s: s < 0)
-    slab_v, slab_f = torch_counts(torch, t[x0:x1 + 1], lambda s: s < 0)
-    A = np.asfortranarray(t[x0:x1 + 1].cpu().numpy())
-    nx = t.shape[0]
-    ex = [(1 - i / (nx - 1)) * 0.0 + (i / (nx - 1)) * 1.0 for i in (x0, x1)]
-    ov, of = oracle.isosurface(A, 'mc', np.float32(0), 1e-3, ((float(ex[0]), float(ex[1])), (0.0, 1.0), (0.0, 1.0)))
-    assert (len(ov), len(of)) == (slab_v, slab_f)
-    gv = v[before_v:before_v + slab_v].cpu().numpy()
-    gf = f[before_f:before_f + slab_f].cpu().numpy()
-    assert np.array_equal(gf - before_v, of)
-    assert np.array_equal(gv[:, 1:], ov[:, 1:].astype(np.float32))  # y, z nodes are the same LinRange
-    err = np.abs(gv[:, 0].astype(np.float64) - ov[:, 0])
-    assert (err <= 2 * np.spacing(np.abs(ov[:, 0]).astype(np.float32))).all(), err.max()
+    A = t.cpu().numpy()
+    assert A.flags['F_CONTIGUOUS'] and A.shape == (1024, 1024, 1024)
+    windows = oracle.mc_xwindows(A, np.float32(0), ((0, 1),) * 3, windows=128)
+    assert_whole_mesh(v.cpu().numpy(), f.cpu().numpy(), windows)
 
 
 def test_fast_path_is_bit_identical_to_fp64(pkg, cuda, sines1024, monkeypatch):
@@ -105,7 +107,7 @@ def test_fast_path_is_bit_identical_to_fp64(pkg, cuda, sines1024, monkeypatch):
     assert torch.equal(v1.view(torch.int32), v2.view(torch.int32))
 
 
-def test_ct_u16_512(pkg, oracle, cuda):
+def test_ct_u16_512_whole_mesh_bit_exact(pkg, oracle, cuda):
     torch = cuda
     import meshing_gb300.fields as fields
     t = fields.ct_like_u16(512)
@@ -114,18 +116,10 @@ def test_ct_u16_512(pkg, oracle, cuda):
     assert v.dtype == torch.float64
     cv, cf = torch_counts(torch, t, lambda s: s.to(torch.int32) < 500)
     assert (v.shape[0], f.shape[0]) == (cv, cf)
-    x0, x1 = 200, 216
-    before_v, before_f = torch_counts(torch, t[:x0 + 1], lambda s: s.to(torch.int32) < 500)
-    slab_v, slab_f = torch_counts(torch, t[x0:x1 + 1], lambda s: s.to(torch.int32) < 500)
-    A = np.asfortranarray(t[x0:x1 + 1].cpu().numpy())
-    ex = [(1 - i / 511) * -1.0 + (i / 511) * 1.0 for i in (x0, x1)]
-    ov, of = oracle.isosurface(A, 'mc', 500, 1e-3, ((float(ex[0]), float(ex[1])), (-1.0, 1.0), (-1.0, 1.0)))
-    assert (len(ov), len(of)) == (slab_v, slab_f)
-    gv = v[before_v:before_v + slab_v].cpu().numpy()
-    gf = f[before_f:before_f + slab_f].cpu().numpy()
-    assert np.array_equal(gf - before_v, of)
-    assert np.array_equal(gv[:, 1:], ov[:, 1:])
-    assert np.abs(gv[:, 0] - ov[:, 0]).max() <= 1e-12
+    A = t.cpu().numpy()
+    assert A.flags['F_CONTIGUOUS']
+    windows = oracle.mc_xwindows(A, 500, ((-1, 1),) * 3, windows=64)
+    assert_whole_mesh(v.cpu().numpy(), f.cpu().numpy(), windows)
 
 
 @pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
@@ -144,3 +138,37 @@ def test_tma_walk_matches_global_load_walk(pkg, cuda, alg, monkeypatch):
     ctx.close()
     assert f1.shape[0] > 0
     assert torch.equal(f1, f2) and torch.equal(v1, v2)
+
+
+def test_u8_1700_past_2_32_samples_whole_mesh_bit_exact(pkg, oracle, cuda):
+    # 1700^3 UInt8 = 4.91 G samples (more than 2^32): every 64-bit sample,
+    # piece, list and output index path, and the walks' segment-relative
+    # 32-bit offsets, against the oracle over the whole volume.  Three
+    # low-frequency plane waves give surface through the whole volume; the
+    # Float32 iso makes the quotient Float32 with UInt8 differences wrapping.
+    torch = cuda
+    import math
+    n = 1700
+    rng = np.random.default_rng(17)
+    g = torch.linspace(0.0, 1.0, n, dtype=torch.float64, device='cuda').to(torch.float32)
+    terms = []
+    for _ in range(3):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        terms.append((rng.uniform(1, 2) * d, rng.uniform(0, 2 * math.pi)))
+    vol = torch.empty((n, n, n), dtype=torch.uint8, device='cuda')   # [z, y, x]
+    for k in range(n):
+        acc = torch.zeros((n, n), dtype=torch.float32, device='cuda')
+        for w, ph in terms:
+            acc += torch.sin((2 * math.pi * w[0]) * g[None, :] + (2 * math.pi * w[1]) * g[:, None]
+                             + float(2 * math.pi * w[2] * g[k].item() + ph))
+        vol[k] = (acc * 40 + 128).round_().clamp_(0, 255).to(torch.uint8)
+    t = vol.permute(2, 1, 0)
+    iso = np.float32(127.5)
+    m = pkg.MarchingCubes(iso=iso)
+    v, f = run_device(torch, pkg, t, m, ((np.float32(0), np.float32(1)),) * 3)
+    assert v.dtype == torch.float32 and v.shape[0] > 0
+    A = t.cpu().numpy()
+    assert A.flags['F_CONTIGUOUS'] and A.size > 2 ** 32
+    windows = oracle.mc_xwindows(A, iso, ((np.float32(0), np.float32(1)),) * 3, windows=200)
+    assert_whole_mesh(v.cpu().numpy(), f.cpu().numpy(), windows)

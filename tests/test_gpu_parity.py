@@ -72,6 +72,17 @@ def test_sphere64_f64(pkg, oracle, cuda, alg):
         assert (len(v), len(f)) == (8978, 17952)
 
 
+@pytest.mark.parametrize('device', [False, True])
+def test_noisy_spheres_kat(pkg, oracle, cuda, device):
+    # test/runtests.jl:152-172: MarchingTetrahedra(iso=8.0) on 21^3 noisy
+    # distances (Julia 1.9's MersenneTwister(0) stream, restated in
+    # oracle/julia_rand.py) gives 3466 vertices and 6928 faces; the CUDA path
+    # gives the oracle's mesh bit for bit
+    import julia_rand
+    v, f = check(pkg, oracle, julia_rand.noisy_spheres(), 'mt', iso=8.0, device=device)
+    assert (len(v), len(f)) == (3466, 6928)
+
+
 @pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
 def test_device_and_host_paths_agree(pkg, oracle, cuda, alg):
     A = sphere(40, 0.55, np.float32)

@@ -335,3 +335,42 @@ def test_welded_mc_sphere_is_a_closed_sphere(oracle, n, r):
     p = v[f - 1]
     vol = np.einsum('ij,ij->i', p[:, 0], np.cross(p[:, 1], p[:, 2])).sum() / 6
     assert abs(vol / (4 / 3 * np.pi * r ** 3) - 1) < 0.01
+
+
+def test_julia_mersenne_twister_stream():
+    # rand(MersenneTwister(0), 3) of Julia 1.9 (the values Julia's own
+    # documentation examples print for this seed)
+    import julia_rand
+    assert julia_rand.rand_mersenne_twister(0, 3).tolist() == [0.8236475079774124, 0.9103565379264364,
+                                                               0.16456579813368521]
+
+
+@pytest.mark.parametrize('restatement', ['c', 'python'])
+def test_noisy_spheres_kat(oracle, restatement):
+    # test/runtests.jl:152-172: MarchingTetrahedra(iso=8.0) on the noisy distance
+    # field gives 3466 vertices and 6928 faces
+    import julia_rand
+    vol = julia_rand.noisy_spheres()
+    assert vol.dtype == np.float64 and vol.shape == (21, 21, 21)
+    run = oracle.isosurface if restatement == 'c' else pyoracle.isosurface
+    v, f = run(vol, 'mt', 8.0)
+    assert (len(v), len(f)) == (3466, 6928)
+
+
+@pytest.mark.parametrize('dt,iso,rg', [(np.float32, np.float32(0.1), ((0, 1),) * 3), (np.uint16, 500, ((-1, 1),) * 3),
+                                       (np.float64, 0.0, ((-1.0, 2.5), (0.0, 1.0), (0.0, 1.0)))])
+def test_mc_x_windows_concatenate_to_the_whole_mesh(oracle, dt, iso, rg):
+    # the reference's MC loop is x-outermost (src/marching_cubes.jl:40): the
+    # meshes of consecutive x windows of cells, with the whole volume's nodes,
+    # are consecutive blocks of the whole mesh
+    rng = np.random.default_rng(5)
+    if dt == np.uint16:
+        A = np.asfortranarray(rng.integers(0, 1000, (37, 20, 23)).astype(dt))
+    else:
+        A = np.asfortranarray(rng.standard_normal((37, 20, 23)).astype(dt))
+    v, f = oracle.isosurface(A, 'mc', iso, 1e-3, rg)
+    ws = oracle.mc_xwindows(A, iso, rg, windows=9, threads=3)
+    assert [w[0] for w in ws] == [0] + [w[1] for w in ws[:-1]] and ws[-1][1] == 36
+    off = np.cumsum([0] + [len(w[2]) for w in ws[:-1]])
+    assert np.array_equal(np.concatenate([w[2] for w in ws]).view(np.uint8), v.view(np.uint8))
+    assert np.array_equal(np.concatenate([w[3] + o for w, o in zip(ws, off)]), f)
