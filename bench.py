@@ -15,9 +15,22 @@ Metric: Gvoxels/s counting input samples nx*ny*nz.
 The roofline object reports the dominant kernel's algorithmic bytes over its
 CUDA-event time; `pipeline` reports in+out bytes over the whole step.
 
+On one GPU the same JSON line also carries the suite's other workloads, each
+with its own clock record (`--no-extras` leaves them out; `--workload X` runs
+one of them alone):
+  batched -- 4096 uneven Float32 volumes in one tuned, graph-replayed batch,
+             against a loop of per-volume calls;
+  serving -- Poisson arrivals of mixed requests (32^3..512^3, Float32/Float64,
+             60/30/10 MC/MT/NSN) under a 120 GB budget, the offered rate
+             doubled until the loop saturates; 128^3 MC requests against a
+             batch of the same 256 distinct volumes;
+  gyroid  -- MC, MT and NSN on the Float32 256^3 gyroid;
+  ct      -- MC on the UInt16 512^3 CT-like volume.
+
 --impl reference times the reference algorithm on the host cores instead:
 the CPU restatement of Meshing.jl's MarchingCubes (single-threaded, as the
-reference is) on a z slab of the same field.
+reference is) on a z slab from the middle of the same field; the in-line
+cpu_baseline times the same slab.
 Multi-GPU (torchrun): independent replicas, weak scaling.
 """
 import argparse
@@ -25,6 +38,7 @@ import ctypes
 import json
 import math
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -191,39 +205,89 @@ def host_link(hvol, hv, hf, dev):
     return out
 
 
-def cpu_baseline(n, planes, steps=1, warmup=0):
-    """Oracle (CPU restatement of MarchingCubes) on a z slab of the field: Gvoxels/s."""
+def host_cpu():
+    """CPU model and core count of this host, and whether Julia (Meshing.jl's
+    language) is installed."""
+    model = None
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        fields = dict((a.strip(), b.strip()) for a, b in (ln.split(':', 1) for ln in out.splitlines() if ':' in ln))
+        model = fields.get('Model name') or fields.get('Vendor ID')
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for line in open('/proc/cpuinfo'):
+                if line.lower().startswith('model name'):
+                    model = line.split(':', 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    julia = shutil.which('julia')
+    return {'cpu_model': model or 'unknown', 'host_cores': os.cpu_count(),
+            'meshing_jl': ('julia found at %s (not used: the restatement is timed)' % julia) if julia else
+            'Meshing.jl: unavailable on this box (no Julia)'}
+
+
+# The CPU sample: CPU_PLANES z cell planes from the middle of the benchmark
+# volume, the same slab for the reference arm and the in-line cpu_baseline.
+CPU_PLANES = 96
+
+
+def cpu_slab(n, planes):
+    """Fortran view (n, n, planes + 1) of z planes from the middle of the field."""
+    z0 = max(0, (n - (planes + 1)) // 2)
+    slab = sines_host(n, z0, planes + 1)         # C-ordered (nz, n, n) == Julia layout (n, n, nz)
+    return slab.transpose(2, 1, 0), z0
+
+
+def cpu_baseline(n, planes, steps=1, warmup=0, threads=1):
+    """Oracle (CPU restatement of MarchingCubes) on a z slab of the field: Gvoxels/s.
+    threads > 1 splits the slab into x windows meshed on that many threads."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle
-    slab = sines_host(n, 0, planes + 1)          # C-ordered (nz, n, n) == Julia layout (n, n, nz)
-    A = slab.transpose(2, 1, 0)                  # Fortran view, shape (n, n, nz)
-    # z coordinates of the slab: the same LinRange nodes as the full grid's first planes,
-    # which only changes vertex positions, not the work done
+    A, z0 = cpu_slab(n, planes)
+    # the slab's z coordinates are its own LinRange nodes, which changes vertex
+    # positions only, not the work done
     rng = ((0, 1), (0, 1), (0, 1))
+    if threads > 1:
+        A = np.asfortranarray(A)
+        run = lambda: oracle.mc_xwindows(A, np.float32(0), rng, windows=4 * threads, threads=threads)
+    else:
+        run = lambda: oracle.isosurface(A, 'mc', np.float32(0), 1e-3, rng)
     for _ in range(warmup):
-        oracle.isosurface(A, 'mc', np.float32(0), 1e-3, rng)
-    t0 = time.perf_counter()
+        run()
+    times = []
     for _ in range(steps):
-        v, f = oracle.isosurface(A, 'mc', np.float32(0), 1e-3, rng)
-    dt = (time.perf_counter() - t0) / steps
+        t0 = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - t0)
+    dt = sum(times) / len(times)
     vox = float(n) * n * (planes + 1)
-    return vox / dt / 1e9, dt, len(v), len(f), vox
+    return vox / dt / 1e9, dt, vox, z0
+
+
+def cpu_sample_text(n, planes, z0, dt, threads):
+    return ('z slab %dx%dx%d (planes %d..%d, %.0f M samples) of the benchmark field, CPU restatement of '
+            'MarchingCubes (oracle/oracle.c; %s), %.2f s per pass' % (
+                n, n, planes + 1, z0, z0 + planes, n * n * (planes + 1) / 1e6,
+                'single-threaded like Meshing.jl' if threads == 1 else
+                'x windows on %d threads' % threads, dt))
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    planes = args.cpu_planes or 32
-    val, dt, nv, nf, vox = cpu_baseline(args.n, planes, steps=args.steps, warmup=args.warmup)
-    sample = ('z slab %dx%dx%d (%.0f M samples) of the benchmark field, CPU restatement of MarchingCubes '
-              '(oracle/oracle.c, single-threaded like Meshing.jl), %.2f s per step' %
-              (args.n, args.n, planes + 1, vox / 1e6, dt))
+    planes = args.cpu_planes or CPU_PLANES
+    val, dt, vox, z0 = cpu_baseline(args.n, planes, steps=args.steps, warmup=args.warmup)
+    info = host_cpu()
     line = {'impl': 'reference', 'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes',
             'value': val, 'unit': 'Gvoxels/s', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': dt * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': WORKLOAD % args.n, 'sample_planes': planes + 1},
-            'cpu_baseline': {'value': val, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port', 'sample': sample},
+            'config': {'workload': WORKLOAD % args.n, 'sample_planes': planes + 1, 'sample_z0': z0},
+            'cpu_baseline': {'value': val, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port',
+                             'sample': cpu_sample_text(args.n, planes, z0, dt, 1), **info},
             'e2e': {'value': val, 'unit': 'Gvoxels/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
 
@@ -315,6 +379,21 @@ def run_ours(args, rank, world, dist):
     link = host_link(hvol, hv, hf, dev)  # overwrites hv / hf: after the check
 
     ms, e2e_ms = max_over_ranks(dist, [ms, e2e_ms], dev)
+    # the other workloads of the benchmark suite, each with its own clock record
+    # (one GPU only: replicas of a scaling run time the headline alone)
+    extras = {}
+    if world == 1 and not args.no_extras:
+        ctx.close()
+        del hvol, hv, hf, vol, verts, faces, counts
+        torch.cuda.empty_cache()
+        for key, fn in (('batched', measure_batched), ('serving', measure_serving), ('gyroid', measure_gyroid),
+                        ('ct', measure_ct)):
+            t0 = time.time()
+            try:
+                extras[key] = fn(args, rank, world, dev)
+            except Exception as e:  # a failed side workload is reported, the headline stands
+                extras[key] = {'error': '%s: %s' % (type(e).__name__, e)}
+            print('bench: %s took %.1f s' % (key, time.time() - t0), file=sys.stderr, flush=True)
     if rank != 0:
         return
     vox = float(n) ** 3
@@ -351,11 +430,19 @@ def run_ours(args, rank, world, dist):
     pipe_gbs = (in_b + out_b) / (ms * 1e-3) / 1e9
     cpu = None
     if world == 1 and not args.no_cpu:
-        planes = args.cpu_planes or 600
-        cval, cdt, _, _, cvox = cpu_baseline(n, planes)
+        # the reference arm's slab, passes repeated to about 10-30 s of CPU work
+        planes = args.cpu_planes or CPU_PLANES
+        cval, cdt, _, z0 = cpu_baseline(n, planes, steps=args.cpu_passes)
         cpu = {'value': cval, 'unit': 'Gvoxels/s', 'cores': 1, 'kind': 'port',
-               'sample': 'z slab %dx%dx%d of the same field, CPU restatement of MarchingCubes (oracle/oracle.c, '
-                         'single-threaded like Meshing.jl), %.2f s' % (n, n, planes + 1, cdt)}
+               'sample': cpu_sample_text(n, planes, z0, cdt, 1) + ', mean of %d passes' % args.cpu_passes,
+               **host_cpu()}
+        threads = os.cpu_count() or 1
+        if threads > 1:
+            pval, pdt, _, _ = cpu_baseline(n, planes, steps=2, threads=threads)
+            cpu['all_cores'] = {'value': pval, 'unit': 'Gvoxels/s', 'cores': threads,
+                                'sample': cpu_sample_text(n, planes, z0, pdt, threads),
+                                'note': 'Meshing.jl itself is single-threaded; this is the restatement split '
+                                        'into x windows, for scale'}
     line = {
         'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes',
         'value': whole_job_rate(vox, world, ms) / 1e9,
@@ -378,10 +465,11 @@ def run_ours(args, rank, world, dist):
         'cpu_baseline': cpu,
         'clocks': ck,
     }
+    line.update(extras)
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args, rank, world):
+def measure_batched(args, rank, world, dev):
     """The batched workload: MarchingCubes(iso=0f0) on `--volumes` Float32
     volumes, each axis 16..128, min-union SDFs of 1-8 seeded spheres / boxes on
     [-1,1]^3.  value: one batch (tuned knobs, replayed from a CUDA graph); the
@@ -391,9 +479,7 @@ def run_batched(args, rank, world):
     pkg = ge.load_package()
     import meshing_gb300.fields as fields
     lib = pkg.load_library()
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
+    local = dev.index or 0
     vols = fields.batch_volumes(args.volumes, seed=SEED + rank, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
     m = pkg.MarchingCubes(iso=np.float32(0))
@@ -417,7 +503,6 @@ def run_batched(args, rank, world):
     ms = e0.elapsed_time(e1) / args.steps
     verts, faces, offs = b.outputs()
     o = offs.cpu().numpy()
-
     # a loop of plain per-volume launches into the same layout
     ctx = b.ctx
     p = pkg.make_params(m, (-1, 1), (-1, 1), (-1, 1))
@@ -447,16 +532,19 @@ def run_batched(args, rank, world):
     in_b, out_b = vox * 4, nv * 12 + nf * 24
     peak, peak_kind = measured_peak()
     gbs = (in_b + out_b) / (ms * 1e-3) / 1e9
-    if rank != 0:
-        return
-    line = {
+    knobs = b.knobs
+    del jl, lv, lf, verts, faces, offs
+    b.close()
+    del vols
+    torch.cuda.empty_cache()
+    return {
         'metric': 'Gvoxels/s (input samples per second), batched MarchingCubes', 'workload': 'batched',
         'value': vox * world / (ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32', 'data': 'synthetic',
         'config': {'workload': '%d Float32 volumes, each axis uniform in 16..128, min-union SDF of 1-8 seeded spheres '
-                               '/ boxes on [-1,1]^3, MarchingCubes(iso=0f0)' % len(vols),
-                   'volumes': len(vols), 'samples': int(vox), 'nverts': nv, 'nfaces': nf, 'knobs': b.knobs,
+                               '/ boxes on [-1,1]^3, MarchingCubes(iso=0f0)' % args.volumes,
+                   'volumes': args.volumes, 'samples': int(vox), 'nverts': nv, 'nfaces': nf, 'knobs': knobs,
                    'graph': True, 'l2': 'inputs larger than L2'},
         'loop': {'value': vox / (loop_ms * 1e-3) / 1e9, 'ms_per_step': loop_ms, 'steps': lsteps,
                  'what': 'one mesh_extract_device call per volume, same stream, same outputs',
@@ -467,44 +555,58 @@ def run_batched(args, rank, world):
         'tuner': report.strip().splitlines()[-1],
         'clocks': ck,
     }
-    print(json.dumps(line), flush=True)
 
 
-def run_serving(args, rank, world):
+def run_batched(args, rank, world):
+    import torch
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    line = measure_batched(args, rank, world, torch.device('cuda', local))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_serving(args, rank, world, dev):
     """The serving workload: Poisson arrivals of requests whose cubic size is
     log-uniform in 32..512, 50/50 Float32 / Float64, fields of the plain
     (random sines on [0,1]^3) and batched (primitive SDFs on [-1,1]^3)
     generators, 60/30/10 MarchingCubes / MarchingTetrahedra / NaiveSurfaceNets,
-    answered by the serving loop under a device-memory budget; then 128^3
-    Marching Cubes requests alone, against a batch of the same volumes."""
+    answered by the serving loop under a device-memory budget and a bounded
+    queue.  The offered rate doubles from --rate0 until the loop saturates
+    (served below 90% of offered, or requests rejected) and one rate past that.
+    Then 128^3 MarchingCubes requests over 256 distinct volumes of the batched
+    generator, against one graph-replayed batch of the same 256 volumes."""
     import torch
     import __graft_entry__ as ge
     pkg = ge.load_package()
     import meshing_gb300.fields as fields
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
+    local = dev.index or 0
     rng = np.random.default_rng(SEED + rank)
     pool = []
     for k in range(args.pool):
         n = int(round(math.exp(rng.uniform(math.log(32), math.log(512)))))
         dt = torch.float32 if k % 2 == 0 else torch.float64
         if rng.random() < 0.5:
-            pool.append((fields.sines(n, seed=k, dtype=dt, device='cuda'), ((0, 1),) * 3))
+            pool.append((fields.sines(n, seed=k, dtype=dt, device=dev), ((0, 1),) * 3))
         else:
-            pool.append((fields.primitives_sdf((n, n, n), fields.primitives_params(rng), dtype=dt), ((-1, 1),) * 3))
+            pool.append((fields.primitives_sdf((n, n, n), fields.primitives_params(rng), dtype=dt, device=dev),
+                         ((-1, 1),) * 3))
     torch.cuda.synchronize()
 
     def method(a, dt):
         iso = np.float32(0) if dt == torch.float32 else 0.0
         return [pkg.MarchingCubes, pkg.MarchingTetrahedra, pkg.NaiveSurfaceNets][a](iso=iso)
 
-    srv = pkg.Server(budget_bytes=int(args.budget_gb * 1e9), slots=3, max_wave=256)
+    srv = pkg.Server(budget_bytes=int(args.budget_gb * 1e9), slots=3, max_wave=256, max_queue=args.max_queue,
+                     device=local)
     # warm-up (pinned staging, context scratch, kernel caches), not measured
     warm = [(A, method(a, A.dtype), r) for A, r in pool for a in range(3)]
     srv.replay(warm, np.zeros(len(warm)))
+    clocks = Clocks(local) if rank == 0 else None
     sweep = []
-    for rate in [float(x) for x in args.rates.split(',')]:
-        nreq = int(min(args.requests, max(50, rate * 3)))
+    rate, past = args.rate0, 0
+    while len(sweep) < args.max_rates and past < 2:
+        nreq = int(min(args.requests, max(200, rate * 3)))
         reqs = []
         for _ in range(nreq):
             A, r = pool[int(rng.integers(len(pool)))]
@@ -516,38 +618,47 @@ def run_serving(args, rank, world):
         st = srv.stats()
         print('serving mixed %.0f/s: %d requests in %.1f s, %.1f per wave' % (
             rate, nreq, time.time() - t0, st['requests_per_wave']), file=sys.stderr, flush=True)
+        thr = st['completed'] / st['wall_s'] if st['wall_s'] else 0
         sweep.append({'offered_per_s': rate, 'requests': nreq, 'completed': int(st['completed']),
                       'rejected': int(st['rejected']), 'failed': int(st['failed']),
-                      'throughput_per_s': st['completed'] / st['wall_s'] if st['wall_s'] else 0,
+                      'rejection_rate': st['rejected'] / nreq,
+                      'throughput_per_s': thr,
                       'gvox_per_s': st['samples'] / st['wall_s'] / 1e9 if st['wall_s'] else 0,
                       'p50_ms': st['p50_ms'], 'p99_ms': st['p99_ms'], 'mean_ms': st['mean_ms'],
                       'peak_reserved_gb': st['peak_reserved_bytes'] / 1e9,
                       'requests_per_wave': st['requests_per_wave']})
-    del pool
+        if past or st['rejected'] > 0 or thr < 0.9 * rate:
+            past += 1
+        rate *= 2
+    del pool, warm, reqs
+    ck_mixed = clocks.stop() if clocks else None
+    torch.cuda.empty_cache()
 
-    # 128^3 Marching Cubes requests: the serving loop against one batch of them
-    vols = [fields.primitives_sdf((128, 128, 128), fields.primitives_params(rng), dtype=torch.float32)
-            for _ in range(16)]
+    # 128^3 Marching Cubes requests: the serving loop against one batch of the same volumes
+    nvol = 256
+    vols = [fields.primitives_sdf((128, 128, 128), fields.primitives_params(rng), dtype=torch.float32, device=dev)
+            for _ in range(nvol)]
     m = pkg.MarchingCubes(iso=np.float32(0))
-    b = pkg.Batch([vols[i % 16] for i in range(256)], m)
+    b = pkg.Batch(vols, m)
     b.count()
     b.set_graph(True)
     for _ in range(3):
         b.run()
     b.sync()
+    clocks = Clocks(local) if rank == 0 else None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(10):
         b.run()
     e1.record()
     torch.cuda.synchronize()
-    batched = 256 * 128 ** 3 / (e0.elapsed_time(e1) / 10 * 1e-3) / 1e9
+    batched = nvol * 128 ** 3 / (e0.elapsed_time(e1) / 10 * 1e-3) / 1e9
     b.close()
     uniform = []
-    srv.replay([(v, m, ((-1, 1),) * 3) for v in vols] * 16, np.zeros(256))  # warm-up, not measured
+    srv.replay([(v, m, ((-1, 1),) * 3) for v in vols], np.zeros(nvol))  # warm-up, not measured
     for rate in [float(x) for x in args.rates128.split(',')]:
         nreq = int(min(args.requests128, max(200, rate * 2)))
-        reqs = [(vols[int(rng.integers(16))], m, ((-1, 1),) * 3) for _ in range(nreq)]
+        reqs = [(vols[int(rng.integers(nvol))], m, ((-1, 1),) * 3) for _ in range(nreq)]
         arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
         srv.reset_stats()
         t0 = time.time()
@@ -557,27 +668,48 @@ def run_serving(args, rank, world):
             rate, nreq, time.time() - t0, st['requests_per_wave']), file=sys.stderr, flush=True)
         g = st['samples'] / st['wall_s'] / 1e9 if st['wall_s'] else 0
         uniform.append({'offered_per_s': rate, 'requests': nreq, 'completed': int(st['completed']),
+                        'rejected': int(st['rejected']), 'rejection_rate': st['rejected'] / nreq,
                         'throughput_per_s': st['completed'] / st['wall_s'] if st['wall_s'] else 0,
                         'gvox_per_s': g, 'fraction_of_batched': g / batched, 'p50_ms': st['p50_ms'],
                         'p99_ms': st['p99_ms'], 'requests_per_wave': st['requests_per_wave']})
+    ck_128 = clocks.stop() if clocks else None
     srv.close()
-    if rank != 0:
-        return
+    del vols, reqs
+    torch.cuda.empty_cache()
     best = max(sweep, key=lambda x: x['gvox_per_s'])
-    line = {
+    ok128 = [u for u in uniform if u['p99_ms'] < 10.0 and u['rejected'] == 0]
+    return {
         'metric': 'Gvoxels/s (input samples per second), serving loop', 'workload': 'serving',
         'value': best['gvox_per_s'], 'unit': 'Gvoxels/s', 'n_gpus': world, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32/f64', 'data': 'synthetic',
         'config': {'workload': 'Poisson arrivals; cubic sizes log-uniform 32..512; 50/50 Float32 / Float64; random '
                                'sines on [0,1]^3 or primitive SDFs on [-1,1]^3; 60/30/10 MC / MT / NSN; iso 0',
-                   'budget_gb': args.budget_gb, 'slots': 3, 'max_wave': 256, 'volume_pool': args.pool},
+                   'budget_gb': args.budget_gb, 'slots': 3, 'max_wave': 256, 'max_queue': args.max_queue,
+                   'volume_pool': args.pool},
         'sweep': sweep,
-        'uniform_128_mc': {'batched_gvox_per_s': batched, 'points': uniform},
+        'saturation_per_s': max(x['throughput_per_s'] for x in sweep),
+        'clocks': ck_mixed,
+        'uniform_128_mc': {'batched_gvox_per_s': batched,
+                           'batched_what': '%d distinct 128^3 Float32 volumes of the batched generator (min-union '
+                                           'SDFs of 1-8 spheres / boxes), one graph-replayed batch' % nvol,
+                           'requests_over': 'the same %d volumes, drawn uniformly' % nvol,
+                           'points': uniform,
+                           'best_fraction_with_p99_under_10ms': max((u['fraction_of_batched'] for u in ok128),
+                                                                    default=None),
+                           'clocks': ck_128},
     }
-    print(json.dumps(line), flush=True)
 
 
-def run_ct(args, rank, world):
+def run_serving(args, rank, world):
+    import torch
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    line = measure_serving(args, rank, world, torch.device('cuda', local))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_ct(args, rank, world, dev):
     """MarchingCubes(iso=500) on the UInt16 512^3 CT-like volume: background
     N(100, 20) clamped to >= 0 plus 3 seeded ellipsoidal shells N(1000, 50), 4
     voxels thick (X = Y = Z = -1:1; UInt16 differences wrap).  Device time per
@@ -587,10 +719,10 @@ def run_ct(args, rank, world):
     pkg = ge.load_package()
     import meshing_gb300.fields as fields
     n = args.n if args.n != N_DEFAULT else 512
-    t = fields.ct_like_u16(n, seed=SEED)
+    t = fields.ct_like_u16(n, seed=SEED, device=dev)
     torch.cuda.synchronize()
     m = pkg.MarchingCubes(iso=500)
-    ctx = pkg.Context(0)
+    ctx = pkg.Context(dev.index or 0)
     v, f = pkg.isosurface(t, m, ctx=ctx)
     verts, faces = torch.empty_like(v), torch.empty_like(f)
     for _ in range(args.warmup):
@@ -599,12 +731,14 @@ def run_ct(args, rank, world):
     ctx.stage_times()
     ctx.enable_timing(True)
     stream = torch.cuda.current_stream()
+    clocks = Clocks(dev.index or 0) if rank == 0 else None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
         pkg.isosurface_device(t, m, verts=verts, faces=faces, ctx=ctx)
     e1.record(stream)
     torch.cuda.synchronize()
+    ck = clocks.stop() if clocks else None
     ctx.sync()
     ms = e0.elapsed_time(e1) / args.steps
     st = {k: v_[0] / args.steps for k, v_ in ctx.stage_times().items() if v_[1]}
@@ -617,20 +751,31 @@ def run_ct(args, rank, world):
             'expand': (st.get('expand', 0), out_b)}
     roof = {k: {'ms': t_, 'gbs': b / (t_ * 1e-3) / 1e9 if t_ else None,
                 'frac': b / (t_ * 1e-3) / 1e9 / peak if t_ else None} for k, (t_, b) in kern.items()}
+    nv, nf = v.shape[0], f.shape[0]
+    del t, v, f, verts, faces
+    torch.cuda.empty_cache()
+    return {'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes', 'workload': 'ct',
+            'value': n ** 3 / (ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': ms, 'steps': args.steps,
+            'dtype': 'u16', 'data': 'synthetic',
+            'config': {'workload': 'UInt16 %d^3 CT-like volume (N(100,20) background, 3 seeded '
+                                   'ellipsoidal shells N(1000,50)), MarchingCubes(iso=500)' % n,
+                       'nverts': nv, 'nfaces': nf, 'output': 'Float64 vertices',
+                       'stage_ms': st, 'repeatable': bool(ok), 'l2': 'inputs larger than L2'},
+            'kernels': roof, 'peak': peak, 'peak_source': peak_kind,
+            'pipeline': {'bytes': in_b + out_b, 'frac': (in_b + out_b) / (ms * 1e-3) / 1e9 / peak},
+            'clocks': ck}
+
+
+def run_ct(args, rank, world):
+    import torch
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    line = measure_ct(args, rank, world, torch.device('cuda', local))
     if rank == 0:
-        print(json.dumps({'metric': 'Gvoxels/s (input samples per second), plain MarchingCubes', 'workload': 'ct',
-                          'value': n ** 3 / (ms * 1e-3) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': ms,
-                          'dtype': 'u16', 'data': 'synthetic',
-                          'config': {'workload': 'UInt16 %d^3 CT-like volume (N(100,20) background, 3 seeded '
-                                                 'ellipsoidal shells N(1000,50)), MarchingCubes(iso=500)' % n,
-                                     'nverts': v.shape[0], 'nfaces': f.shape[0], 'output': 'Float64 vertices',
-                                     'stage_ms': st, 'repeatable': bool(ok)},
-                          'kernels': roof, 'peak': peak, 'peak_source': peak_kind,
-                          'pipeline': {'bytes': in_b + out_b, 'frac': (in_b + out_b) / (ms * 1e-3) / 1e9 / peak}}),
-              flush=True)
+        print(json.dumps(line), flush=True)
 
 
-def run_gyroid(args, rank, world):
+def measure_gyroid(args, rank, world, dev):
     """MarchingCubes, MarchingTetrahedra and NaiveSurfaceNets, iso 0, on the
     Float32 gyroid sin x cos y + sin y cos z + sin z cos x over [-3pi, 3pi]^3
     (`--n` nodes per axis, 256 by default here): device time per call and per
@@ -640,13 +785,14 @@ def run_gyroid(args, rank, world):
     pkg = ge.load_package()
     import meshing_gb300.fields as fields
     n = args.n if args.n != N_DEFAULT else 256
-    t = fields.gyroid(n, dtype=torch.float32)
+    t = fields.gyroid(n, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
     r = (-3 * math.pi, 3 * math.pi)
+    peak, peak_kind = measured_peak()
     out = {}
     for name, m in (('MarchingCubes', pkg.MarchingCubes(iso=0.0)), ('MarchingTetrahedra', pkg.MarchingTetrahedra(iso=0.0)),
                     ('NaiveSurfaceNets', pkg.NaiveSurfaceNets(iso=0.0))):
-        ctx = pkg.Context(0)
+        ctx = pkg.Context(dev.index or 0)
         v, f = pkg.isosurface(t, m, r, r, r, ctx=ctx)
         verts, faces = torch.empty_like(v), torch.empty_like(f)
         for _ in range(args.warmup):
@@ -654,23 +800,49 @@ def run_gyroid(args, rank, world):
         ctx.sync()
         ctx.stage_times()
         ctx.enable_timing(True)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
+        # the 64 MiB volume fits in L2: every timed call follows a write of a buffer
+        # larger than L2, and only the calls are timed (CUDA events around each)
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+        clocks = Clocks(dev.index or 0) if rank == 0 else None
+        evs = []
         for _ in range(args.steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
             pkg.isosurface_device(t, m, r, r, r, verts=verts, faces=faces, ctx=ctx)
-        e1.record()
+            e1.record()
+            evs.append((e0, e1))
         torch.cuda.synchronize()
+        ck = clocks.stop() if clocks else None
         ctx.sync()
-        ms = e0.elapsed_time(e1) / args.steps
+        ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+        del flush
         st = {k: v[0] / args.steps for k, v in ctx.stage_times().items() if v[1]}
         ok = torch.equal(verts, v) and torch.equal(faces, f)
+        # bytes in (Float32 samples) + bytes out (Float64 vertices: the Float64 iso; Int64 faces)
+        io = n ** 3 * 4 + v.shape[0] * 24 + f.shape[0] * 24
         out[name] = {'ms_per_call': ms, 'gvox_per_s': n ** 3 / (ms * 1e-3) / 1e9, 'nverts': v.shape[0],
-                     'nfaces': f.shape[0], 'stage_ms': st, 'repeatable': bool(ok)}
+                     'nfaces': f.shape[0], 'stage_ms': st, 'repeatable': bool(ok),
+                     'roofline': {'bytes': io, 'achieved': io / (ms * 1e-3) / 1e9,
+                                  'frac': io / (ms * 1e-3) / 1e9 / peak, 'unit': 'GB/s'},
+                     'clocks': ck}
         ctx.close()
+        del v, f, verts, faces
+    del t
+    torch.cuda.empty_cache()
+    return {'metric': 'Gvoxels/s per algorithm', 'workload': 'gyroid', 'n': n, 'dtype': 'f32', 'steps': args.steps,
+            'config': {'workload': 'Float32 %d^3 gyroid over [-3pi,3pi]^3, iso 0.0 (Float64)' % n,
+                       'l2': 'L2 flushed before every timed call (a 512 MiB write); calls timed one by one'},
+            'peak': peak, 'peak_source': peak_kind, 'algorithms': out}
+
+
+def run_gyroid(args, rank, world):
+    import torch
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    line = measure_gyroid(args, rank, world, torch.device('cuda', local))
     if rank == 0:
-        print(json.dumps({'metric': 'Gvoxels/s per algorithm', 'workload': 'gyroid', 'n': n, 'dtype': 'f32',
-                          'config': {'workload': 'Float32 %d^3 gyroid over [-3pi,3pi]^3, iso 0.0 (Float64)' % n},
-                          'algorithms': out}), flush=True)
+        print(json.dumps(line), flush=True)
 
 
 def main():
@@ -681,17 +853,25 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--n', type=int, default=N_DEFAULT, help='grid size per axis (default 1024)')
     ap.add_argument('--cpu-planes', type=int, default=None,
-                    help='z cell planes of the CPU sample (default 600, about 12 s on one core; 32 per step for --impl reference)')
+                    help='z cell planes of the CPU sample (default %d, about 2-3 s per pass on one core)' % CPU_PLANES)
+    ap.add_argument('--cpu-passes', type=int, default=6, help='passes over the CPU sample for cpu_baseline')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    ap.add_argument('--no-extras', action='store_true',
+                    help='plain workload only: skip the batched, serving, gyroid and CT results of the default line')
     ap.add_argument('--workload', default='plain', choices=['plain', 'batched', 'serving', 'gyroid', 'ct'],
                     help='plain: one 1024^3 volume (the headline); batched: many uneven volumes; serving: the '
                          'serving loop under Poisson arrivals')
     ap.add_argument('--volumes', type=int, default=4096, help='volumes of the batched workload')
     ap.add_argument('--pool', type=int, default=40, help='serving: distinct resident request volumes')
     ap.add_argument('--budget-gb', type=float, default=120.0, help='serving: device memory budget')
-    ap.add_argument('--rates', default='100,400,1600', help='serving: offered requests per second')
-    ap.add_argument('--requests', type=int, default=1200, help='serving: requests per rate (at most)')
-    ap.add_argument('--rates128', default='60000,145000,175000', help='serving 128^3: offered requests per second')
+    ap.add_argument('--rate0', type=float, default=400.0,
+                    help='serving: first offered rate (requests per second); doubled until the loop saturates')
+    ap.add_argument('--max-rates', type=int, default=8, help='serving: at most this many offered rates')
+    ap.add_argument('--max-queue', type=int, default=1024, help='serving: waiting requests beyond which the loop '
+                                                                'rejects (MESH_EBUSY)')
+    ap.add_argument('--requests', type=int, default=1500, help='serving: requests per rate (at most)')
+    ap.add_argument('--rates128', default='60000,120000,160000,200000',
+                    help='serving 128^3: offered requests per second')
     ap.add_argument('--requests128', type=int, default=60000, help='serving 128^3: requests per rate (at most)')
     args = ap.parse_args()
     world = int(os.environ.get('WORLD_SIZE', '1'))
