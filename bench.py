@@ -402,23 +402,30 @@ def run_ours(args, rank, world, dist):
     out_b = nv * 12 + nf * 24
     stage = {k: v[0] / args.steps for k, v in st.items()}  # each timed step runs every stage once
     # algorithmic bytes per launch (input 4 B per sample, mesh 12 B per vertex and
-    # 24 B per face): classify (k_classify) and compact (k_compact_mc, the second
-    # pass over the volume that lists the active cells) each read every sample;
-    # expand (k_expand_mc) writes the mesh; the scan reads 3 u32 counts and writes
-    # 3 int64 bases per piece.  The active-cell list between compaction and
-    # expansion is not counted.
+    # 24 B per face): classify (k_classify) reads every sample; the scan reads 3
+    # u32 counts and writes 3 int64 bases per piece; the direct emission
+    # (k_direct_mc) writes the mesh (its second read of the samples of active
+    # cells is not algorithmic and is not counted).  In the list form
+    # (MESHING_GB300_LIST_EMIT=1) the compaction (k_compact_mc) reads the
+    # samples of the active chunks and writes the list of active cells, and the
+    # expansion (k_expand_mc) writes the mesh: only the expansion gets bytes.
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     kern = {
         'classify': {'ms': stage['classify'], 'bytes': in_b, 'kernel': 'k_classify'},
         'scan': {'ms': stage['scan'], 'bytes': float(pieces(n, n, n, sms) * 3 * (4 + 8)), 'kernel': 'k_scan'},
-        'compact': {'ms': stage['emit'], 'bytes': in_b, 'kernel': 'k_compact_mc'},
-        'expand': {'ms': stage['expand'], 'bytes': float(out_b), 'kernel': 'k_expand_mc'},
     }
+    if stage.get('expand'):
+        kern['compact'] = {'ms': stage['emit'], 'bytes': None, 'kernel': 'k_compact_mc',
+                           'note': 'reads the samples of active chunks, writes the active-cell list'}
+        kern['expand'] = {'ms': stage['expand'], 'bytes': float(out_b), 'kernel': 'k_expand_mc'}
+    else:
+        kern['emit'] = {'ms': stage['emit'], 'bytes': float(out_b), 'kernel': 'k_direct_mc',
+                        'note': 'writes the mesh; its read of the samples of active cells is not counted'}
     for k in kern.values():
-        k['gbs'] = k['bytes'] / (k['ms'] * 1e-3) / 1e9 if k['ms'] else None
+        k['gbs'] = k['bytes'] / (k['ms'] * 1e-3) / 1e9 if k['ms'] and k['bytes'] else None
         k['frac'] = k['gbs'] / peak if k['gbs'] else None
-    # the dominant kernel: the longest launch of the step
-    dom = max(('classify', 'compact', 'expand'), key=lambda k: kern[k]['ms'])
+    # the dominant kernel: the longest launch of the step (that has algorithmic bytes)
+    dom = max((k for k in kern if kern[k]['bytes']), key=lambda k: kern[k]['ms'])
     achieved = kern[dom]['gbs']
     traffic = None
     tpath = os.path.join(ROOT, 'profiles', 'traffic.json')
@@ -747,8 +754,11 @@ def measure_ct(args, rank, world, dev):
     peak, peak_kind = measured_peak()
     in_b = float(n) ** 3 * 2
     out_b = v.shape[0] * 24 + f.shape[0] * 24  # Float64 vertices (Int ranges, Int iso)
-    kern = {'classify': (st.get('classify', 0), in_b), 'compact': (st.get('emit', 0), in_b),
-            'expand': (st.get('expand', 0), out_b)}
+    kern = {'classify': (st.get('classify', 0), in_b)}
+    if st.get('expand'):  # list form: compaction, then expansion (writes the mesh)
+        kern['expand'] = (st['expand'], out_b)
+    else:  # direct emission (writes the mesh)
+        kern['emit'] = (st.get('emit', 0), out_b)
     roof = {k: {'ms': t_, 'gbs': b / (t_ * 1e-3) / 1e9 if t_ else None,
                 'frac': b / (t_ * 1e-3) / 1e9 / peak if t_ else None} for k, (t_, b) in kern.items()}
     nv, nf = v.shape[0], f.shape[0]

@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(BUILD, 'libmeshing_gb300.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 SOURCES = ['mesh_api.cu', 'k_tables.cu', 'k_classify.cu', 'k_scan.cu', 'k_walk_mc.cu', 'k_emit_mc.cu',
-           'k_emit_halo.cu', 'mesh_noalloc.cu', 'mesh_batch.cu', 'mesh_serve.cu', 'k_post.cu', 'k_weld.cu']
+           'k_direct_mc.cu', 'k_emit_halo.cu', 'mesh_noalloc.cu', 'mesh_batch.cu', 'mesh_serve.cu', 'k_post.cu', 'k_weld.cu']
 
 
 def nvcc():

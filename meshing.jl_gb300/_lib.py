@@ -138,9 +138,10 @@ class Context:
     def stage_times(self):
         """{stage: (total device ms, kernel launches)} since the last query; stages are
         classify (with MESHING_GB300_ONE_WALK=1, the Marching Cubes walk that also
-        lists the active cells), scan, emit (MC: compaction of the active cells by
-        a second walk; MT/NSN: the whole emit), expand (MC: active cells into
-        vertices and faces)."""
+        lists the active cells), scan, emit (MC: vertices and faces straight from
+        the volume, or with MESHING_GB300_LIST_EMIT=1 the compaction of the active
+        cells by a second walk; MT/NSN: the whole emit), expand (MC list form only:
+        active cells into vertices and faces)."""
         ms = (ctypes.c_double * 4)()
         n = (ctypes.c_int64 * 4)()
         check(self._lib.mesh_ctx_stage_times(self.handle, ms, n), self.handle)

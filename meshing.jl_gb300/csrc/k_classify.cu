@@ -206,16 +206,19 @@ __device__ __forceinline__ void classify_tile_mc_inner(const Plan &p, const uint
         }
         zoff += (uint32_t)(n - (n + U - 1) / U * U) * sxy;  // back to plane zc0 + n after a short chunk
         const int chunk = seg * p.chunks_per_seg + (zc0 - zbeg) / ZC;
-        uint8_t mine = 0;
+        uint32_t mine = 0;  // lane r: the active columns of row y0 + r
 #pragma unroll
         for (int r = 0; r < WY; r++) {
-            const bool act = (__ballot_sync(FULL, pk[r] != 0u) & CELLM) != 0u;
-            if (lane == r) mine = act;
+            const uint32_t am = __ballot_sync(FULL, pk[r] != 0u) & CELLM;
+            if (lane == r) mine = am;
             cv[r] += pk[r] & ((1u << PK_F) - 1u);
             cf[r] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
             ca[r] += pk[r] >> PK_A;
         }
-        if (lane < WY) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+        if (lane < WY) {
+            p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine != 0u;
+            if (p.cmask) p.cmask[((int64_t)tx * p.cy + y0 + lane) * p.nchunks + chunk] = mine;
+        }
     }
     if (lane >= TILE_X) return;
     const int64_t np = p.pstride;
@@ -311,16 +314,19 @@ __device__ __forceinline__ void classify_tile_mc(const Plan &p, const uint32_t *
             }
         }
         const int chunk = seg * p.chunks_per_seg + (zc0 - zbeg) / ZC;
-        uint8_t mine = 0;
+        uint32_t mine = 0;  // lane r: the active columns of row y0 + r (pk holds existing cells only)
 #pragma unroll
         for (int r = 0; r < WY; r++) {
-            const bool act = __any_sync(FULL, pk[r] != 0u);
-            if (lane == r) mine = act;
+            const uint32_t am = __ballot_sync(FULL, pk[r] != 0u);
+            if (lane == r) mine = am;
             cv[r] += pk[r] & ((1u << PK_F) - 1u);
             cf[r] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
             ca[r] += pk[r] >> PK_A;
         }
-        if (lane < WY && y0 + lane < p.cy) p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine;
+        if (lane < WY && y0 + lane < p.cy) {
+            p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine != 0u;
+            if (p.cmask) p.cmask[((int64_t)tx * p.cy + y0 + lane) * p.nchunks + chunk] = mine;
+        }
     }
     if (!cellx) return;
     const int64_t np = p.pstride;
@@ -399,7 +405,7 @@ __device__ __forceinline__ void classify_tile(const Plan &p, const uint32_t *s_t
 }
 
 template <class T, int ALG>
-__global__ void __launch_bounds__(256) k_classify(const Plan p) {
+__global__ void __launch_bounds__(256, 3) k_classify(const Plan p) {
     __shared__ uint32_t s_tab[256];
     if (ALG == MESH_ALG_MC)
         load_tables_mc_packed(s_tab);

@@ -230,6 +230,9 @@ cudaError_t upload_and_classify(mesh_ctx *c) {
     return e;
 }
 
+bool one_walk(const mesh_ctx *c);
+bool direct_mc(const mesh_ctx *c);
+
 int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
             const mesh_params *p) {
     Plan &P = c->plan;
@@ -310,6 +313,12 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     P.cnt = (uint32_t *)c->cnt.ptr;
     P.base = (int64_t *)c->base.ptr;
     P.flags = (uint8_t *)c->flags.ptr;
+    P.cmask = nullptr;
+    if (direct_mc(c)) {
+        const size_t mb = (size_t)P.tiles_x * P.cy * P.nchunks * sizeof(uint32_t);
+        if ((e = c->cmask.ensure(mb)) != cudaSuccess) return cuda_fail(c, e, "mask buffer");
+        P.cmask = (uint32_t *)c->cmask.ptr;
+    }
     P.scan_state = (unsigned long long *)c->scan.ptr;
     P.scan_ticket = (unsigned int *)((char *)c->scan.ptr + sb);
     // misc: totals[NCNT] int64, then the error word, the work counter and the
@@ -396,6 +405,13 @@ bool one_walk(const mesh_ctx *c) {
     return c->plan.alg == MESH_ALG_MC && !c->weld && (c->one_walk || c->host_mapped);
 }
 
+// Marching Cubes emitted straight from the volume (the default): the classify
+// walk leaves per-chunk active-column masks and no list of active cells is
+// built.  The opt-in TMA walk writes no masks and takes the list form.
+bool direct_mc(const mesh_ctx *c) {
+    return c->plan.alg == MESH_ALG_MC && !c->list_emit && !c->want_tma && !one_walk(c);
+}
+
 int run_count(mesh_ctx *c) {
     Plan &P = c->plan;
     cudaError_t e;
@@ -475,6 +491,13 @@ int launch_emit(mesh_ctx *c) {
         count_kernels(c, 3, 1);
         return e != cudaSuccess ? cuda_fail(c, e, "expand launch") : MESH_OK;
     }
+    if (direct_mc(c)) {
+        mark(c, 2);
+        e = launch_direct_mc(c->plan, c->Q64, c->P64, c->stream);
+        mark(c, 2);
+        count_kernels(c, 2, 1);
+        return e != cudaSuccess ? cuda_fail(c, e, "emit launch") : MESH_OK;
+    }
     mark(c, 2);
     if (c->plan.alg == MESH_ALG_MC) e = launch_emit_mc(c->plan, c->Q64, c->P64, 0, c->stream);
     else e = launch_emit_halo(c->plan, c->Q64, c->A64, c->P64, c->stream);
@@ -536,10 +559,14 @@ int emit_pipelined(mesh_ctx *c, int K, void *verts, int64_t *faces) {
         q.ntx = tx[g + 1] - tx[g];
         q.e_lo = E[g];
         q.e_hi = E[g + 1];
-        e = launch_emit_mc(q, c->Q64, c->P64, 0, c->stream);
-        if (e == cudaSuccess && E[g + 1] > E[g]) {
-            e = launch_emit_mc(q, c->Q64, c->P64, 1, c->stream);
-            nexp++;
+        if (direct_mc(c)) {
+            e = launch_direct_mc(q, c->Q64, c->P64, c->stream);
+        } else {
+            e = launch_emit_mc(q, c->Q64, c->P64, 0, c->stream);
+            if (e == cudaSuccess && E[g + 1] > E[g]) {
+                e = launch_emit_mc(q, c->Q64, c->P64, 1, c->stream);
+                nexp++;
+            }
         }
         if (e == cudaSuccess) e = cudaEventRecord(c->ev_part[g], c->stream);
     }
@@ -630,6 +657,8 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     c->want_tma = wt && wt[0] == '1';
     const char *ow = getenv("MESHING_GB300_ONE_WALK");
     c->one_walk = ow && ow[0] == '1';
+    const char *le = getenv("MESHING_GB300_LIST_EMIT");
+    c->list_emit = le && le[0] == '1';
     const char *zc = getenv("MESHING_GB300_ZEROCOPY");
     c->zerocopy = zc && zc[0] == '1';
     const char *pb = getenv("MESHING_GB300_PIPELINE_BYTES");  // <= 0: never pipelined
@@ -644,7 +673,8 @@ void mesh_ctx_destroy(mesh_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->copy) cudaStreamSynchronize(c->copy);
     DevBuf *bufs[] = {&c->vol,   &c->tabs,  &c->cnt, &c->base, &c->flags,    &c->scan,   &c->misc,
-                      &c->out_v, &c->out_f, &c->ent, &c->nrm,  &c->weld_buf, &c->weld_v, &c->gat};
+                      &c->out_v, &c->out_f, &c->ent, &c->nrm,  &c->weld_buf, &c->weld_v, &c->gat,
+                      &c->cmask};
     for (DevBuf *b : bufs) b->release();
     for (cudaEvent_t e : c->ev_part)
         if (e) cudaEventDestroy(e);
@@ -707,7 +737,7 @@ int run_weld(mesh_ctx *c) {
     P.faces_cap = nf;
     P.vkey = (long long *)wb;
     int rc;
-    if ((rc = ensure_entries(c, c->nactive))) return rc;
+    if (!direct_mc(c) && (rc = ensure_entries(c, c->nactive))) return rc;
     if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
     if ((rc = launch_emit(c))) return rc;
     if ((e = launch_weld(P.vkey, nv, P.verts, P.out64, P.faces, nf, (long long *)(wb + o_bsum), c->weld_v.ptr,
@@ -799,7 +829,7 @@ int mesh_fill(mesh_ctx *c, void *verts, int64_t *faces, int out_on_device) {
     P.verts_cap = c->nverts;
     P.faces_cap = c->nfaces;
     int rc;
-    if (P.alg == MESH_ALG_MC && !one_walk(c) && (rc = ensure_entries(c, c->nactive))) return rc;
+    if (P.alg == MESH_ALG_MC && !one_walk(c) && !direct_mc(c) && (rc = ensure_entries(c, c->nactive))) return rc;
     if ((e = cudaMemsetAsync(P.err, 0, sizeof(unsigned), c->stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
     int parts = 1;
     if (!out_on_device && P.alg == MESH_ALG_MC && !one_walk(c) && c->pipe_bytes > 0 &&
@@ -848,7 +878,7 @@ int mesh_extract_device(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t
     P.faces_cap = faces ? faces_cap : 0;
     // an active Marching Cubes cell emits at least 3 vertices; the one walk
     // also leaves up to a block of slots per warp unused
-    if (P.alg == MESH_ALG_MC &&
+    if (P.alg == MESH_ALG_MC && !direct_mc(c) &&
         (rc = ensure_entries(c, P.verts_cap / 3 + (one_walk(c) ? stage_slack(P) : 0))))
         return rc;
     if ((rc = run_count(c))) return rc;

@@ -54,6 +54,7 @@ struct mesh_ctx {
     cudaStream_t stream = nullptr;
     mesh::DevBuf vol, tabs, cnt, base, flags, scan, misc, out_v, out_f, ent;
     mesh::DevBuf nrm;  // mesh_vertex_normals: double accumulators
+    mesh::DevBuf cmask;  // Marching Cubes: per (x tile, cell row, chunk) active-column masks
     // welded Marching Cubes (MESH_ALG_MC_WELDED): the count runs the whole
     // extraction into out_v / out_f and welds it into weld_v; mesh_fill copies
     int weld = 0;
@@ -95,6 +96,10 @@ struct mesh_ctx {
     // expanding the cells in walk order scatters the output writes (1024^3 f32:
     // walk 2.24 + expand 1.41 ms vs classify 1.24 + compact 1.18 + expand 0.75 ms).
     int one_walk = 0;
+    // MESHING_GB300_LIST_EMIT=1: Marching Cubes emitted through the list of
+    // active cells (compaction, then expansion) instead of straight from the
+    // volume (k_direct_mc.cu); kept for comparison tests.
+    int list_emit = 0;
     // MESHING_GB300_ZEROCOPY=1: a Marching Cubes host volume in pinned, mapped
     // memory is read in place over the host link (NVLink-C2C) by the one walk
     // instead of being copied.  Off by default: on GB300 the in-place walk of a

@@ -75,6 +75,9 @@ struct Plan {
     uint32_t *cnt;        // [NCNT][nseg][cy][cx] per-piece vertex / face / active-cell counts
     int64_t *base;        // [NCNT][nseg][cy][cx] exclusive prefix in traversal order
     uint8_t *flags;       // [nchunks][tiles_x][cy] 1 if the tile row has an active cell
+    // Marching Cubes, single volume (null otherwise): [tiles_x][cy][nchunks] bit l
+    // set when cell column tx * TILE_X + l of that row has an active cell in the chunk
+    uint32_t *cmask;
     unsigned long long *scan_state;  // [NCNT][scan tiles] decoupled look-back words
     unsigned int *scan_ticket;
     int64_t *totals;      // [NCNT] total vertices, faces, active cells
@@ -232,6 +235,8 @@ struct GatherIdx {
 cudaError_t launch_gather(const int64_t *src, const GatherIdx &g, int64_t *dst, cudaStream_t s);
 cudaError_t launch_scan(const Plan &p, cudaStream_t s);
 cudaError_t launch_emit(const Plan &p, int Q64, int A64, int P64, cudaStream_t s);
+// Marching Cubes emitted straight from the volume (k_direct_mc.cu): needs cmask.
+cudaError_t launch_direct_mc(const Plan &p, int Q64, int P64, cudaStream_t s);
 // Marching Cubes in one walk: classify + stage entries, then expand them.
 constexpr int STG_BLK = 128;  // staging slots a walking warp takes at a time
 cudaError_t launch_walk_mc(const Plan &p, cudaStream_t s);

@@ -348,3 +348,27 @@ def test_maximum_axis_length(pkg, oracle, cuda, alg, axis):
     with pytest.raises(pkg.MeshError) as ei:
         pkg.isosurface(np.zeros(shape, np.float32, order='F'), method(pkg, alg, np.float32(0.1)))
     assert ei.value.status == 7  # MESH_ETOOLARGE
+
+
+@pytest.mark.parametrize('dt,iso,rg', [(np.float32, np.float32(0.05), ((0, 1),) * 3), (np.float64, 0.0, ((-1, 1),) * 3),
+                                       (np.uint16, 500, ((-1, 1),) * 3), (np.int8, 3, ((-1.0, 1.0),) * 3),
+                                       (np.float16, np.float32(0.1), ((np.float32(-1), np.float32(1)),) * 3)])
+def test_direct_and_list_emission_agree(pkg, oracle, cuda, dt, iso, rg, monkeypatch):
+    # Marching Cubes is emitted straight from the volume by default; the list
+    # form (compaction, then expansion) must give the same mesh, and both the
+    # oracle's.  Shapes: several x tiles, z segments and partial chunks.
+    torch = cuda
+    rng = np.random.default_rng(11)
+    shape = (77, 45, 83)
+    if np.issubdtype(dt, np.integer):
+        info = np.iinfo(dt)
+        A = rng.integers(max(info.min, -200), min(info.max, 1000), shape).astype(dt)
+    else:
+        A = sphere(0, 0.5, dt, shape=shape) + (0.05 * rng.standard_normal(shape)).astype(dt)
+    A = np.asfortranarray(A)
+    got = check(pkg, oracle, A, 'mc', iso=iso, ranges=rg)
+    monkeypatch.setenv('MESHING_GB300_LIST_EMIT', '1')
+    ctx = pkg.Context(0)
+    lst = pkg.isosurface(A, pkg.MarchingCubes(iso=iso), *rg, ctx=ctx)
+    ctx.close()
+    assert np.array_equal(got[1], lst[1]) and np.array_equal(got[0].view(np.uint8), lst[0].view(np.uint8))
