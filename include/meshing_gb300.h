@@ -167,9 +167,9 @@ MESH_API int mesh_ctx_enable_timing(mesh_ctx *ctx, int enable);
 MESH_API int mesh_ctx_stage_times(mesh_ctx *ctx, double *ms, int64_t *launches);
 
 /* No counterpart in the reference.  Extraction for callers that must not
- * allocate: code inside CUDA graph capture (cudaMalloc is illegal there),
- * callbacks of a framework that owns the device memory pool, or real-time
- * loops that must never wait on an allocator.  It does what
+ * allocate: callbacks of a framework that owns the whole device memory pool
+ * (an allocation would compete with it), or real-time loops that must never
+ * block in an allocator.  It does what
  * mesh_extract_device does -- classify, scan, emit, asynchronously on
  * `stream` (a cudaStream_t; NULL = the legacy default stream) -- but calls no
  * allocating routine: the scratch it needs lives in one static device array of
@@ -180,8 +180,10 @@ MESH_API int mesh_ctx_stage_times(mesh_ctx *ctx, double *ms, int64_t *launches);
  * faces_cap were not written).  Marching Cubes reserves room for verts_cap/3
  * active cells, so its scratch grows with verts_cap; a call that needs more
  * scratch than the limit returns MESH_ESCRATCH before any GPU work.  The first
- * call on a device looks up the array's device address (once per device);
- * make that first call before any stream capture.  All calls share the array
+ * call on a device looks up the array's device address (once per device, kept
+ * for the process: after a cudaDeviceReset of that device, do not call it on
+ * that device again); make that first call before any stream capture.  All
+ * calls share the array
  * and it keeps the last call's contents (each call clears what must start at
  * zero), so calls that overlap on the GPU race: serialise them. */
 #define MESH_NOALLOC_SCRATCH_BYTES (64ull << 20)
@@ -228,9 +230,10 @@ MESH_API int mesh_batch_knobs(const mesh_batch *b, int *knobs);
 MESH_API int mesh_batch_tune(mesh_batch *b, int reps, char *report, int report_len);
 
 /* ---- Serving: continuous batching of extraction requests -------------------
- * No counterpart in the reference.  Requests name a device-resident volume and
- * the algorithm parameters (any of the three algorithms, any supported types)
- * and are answered with exactly the mesh isosurface() gives for them alone.
+ * No counterpart in the reference.  Requests name a volume (device or host
+ * memory) and the algorithm parameters (any of the three algorithms, welded
+ * Marching Cubes included, any supported types) and are answered with exactly
+ * the mesh isosurface() gives for them alone.
  * A loop thread admits queued requests in arrival order into waves whenever a
  * slot is free and the device pool (budget_bytes, allocated at creation) can
  * reserve each request's worst-case output: 12 vertices and 5 faces per cell
@@ -245,10 +248,15 @@ MESH_API int mesh_server_create(int device, int64_t budget_bytes, int slots, int
 /* Stops admitting, waits for the waves in flight, frees the pool. */
 MESH_API void mesh_server_destroy(mesh_server *s);
 MESH_API const char *mesh_server_last_error(const mesh_server *s);
-/* Queues a request; *id identifies it.  MESH_EBUDGET: its worst case alone
- * exceeds the budget; MESH_EBUSY: max_queue requests are waiting. */
+/* Queues a request; *id identifies it.  vol_on_device = 0: vol is host memory
+ * (pinned uploads fastest), copied into the pool when the request is admitted
+ * to a wave -- it must stay valid and unchanged until the request has ended;
+ * its bytes count against the budget like the outputs while the request is in
+ * flight.  MESH_EBUDGET: its worst case alone exceeds the budget; MESH_EBUSY:
+ * max_queue requests are waiting.  Welded Marching Cubes requests also use the
+ * slot context's own scratch for the mesh before welding. */
 MESH_API int mesh_server_submit(mesh_server *s, const void *vol, int vol_dtype, int64_t nx, int64_t ny, int64_t nz,
-                                const mesh_params *p, int64_t *id);
+                                int vol_on_device, const mesh_params *p, int64_t *id);
 /* state: 0 queued, 1 running, 2 done, 3 failed (the return value is then the
  * failure's status).  When done: counts and device pointers of the vertices
  * (float(FT) triples) and faces (1-based int64 triples). */

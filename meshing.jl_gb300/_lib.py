@@ -83,7 +83,7 @@ def load():
         'mesh_server_create': (c_int, [c_int, i64, c_int, c_int, c_int, P(vp)]),
         'mesh_server_destroy': (None, [vp]),
         'mesh_server_last_error': (ctypes.c_char_p, [vp]),
-        'mesh_server_submit': (c_int, [vp, vp, c_int, i64, i64, i64, P(MeshParams), P(i64)]),
+        'mesh_server_submit': (c_int, [vp, vp, c_int, i64, i64, i64, c_int, P(MeshParams), P(i64)]),
         'mesh_server_poll': (c_int, [vp, i64, P(c_int), P(i64), P(i64), P(vp), P(vp)]),
         'mesh_server_wait': (c_int, [vp, i64, i64, P(c_int), P(i64), P(i64), P(vp), P(vp)]),
         'mesh_server_release': (c_int, [vp, i64]),

@@ -23,6 +23,7 @@
 #include "mesh_mc.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 namespace mesh {
 
@@ -261,10 +262,27 @@ __global__ void __launch_bounds__(256, COMPACT_MIN_CTAS) k_compact_batch(const P
     }
 }
 
+// Resident CTAs of the compaction and the expansion on the current device, per
+// instantiation, looked up once per device (devices of different models differ).
+template <class T, class Q, class P> void list_grids(int *grid_a, int *grid_b) {
+    constexpr int MAXDEV = 64;
+    static std::mutex mu;
+    static int ga[MAXDEV], gb[MAXDEV];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= MAXDEV) dev = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!ga[dev]) {
+        ga[dev] = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
+        gb[dev] = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>);
+    }
+    *grid_a = ga[dev];
+    *grid_b = gb[dev];
+}
+
 template <class T, class Q, class P> cudaError_t go(const Plan &p, int stage, cudaStream_t s) {
-    // per instantiation: resident CTAs on this device (thread-safe one-time initialisation)
-    static const int grid_a = resident_ctas((const void *)k_compact_mc<T>, 32 * WARPS);
-    static const int grid_b = expand_ctas((const void *)k_expand_mc<T, Q, P, EXP_ORDERED>);
+    int grid_a = 0, grid_b = 0;
+    list_grids<T, Q, P>(&grid_a, &grid_b);
     if (stage == 0) {
         const int nitems = (p.ntx > 0 ? p.ntx : p.tiles_x) * ((p.cy + CR - 1) / CR) * p.nseg;
         cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);

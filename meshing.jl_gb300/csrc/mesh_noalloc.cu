@@ -1,10 +1,9 @@
 // mesh_extract_noalloc: isosurface extraction that allocates nothing.
 //
 // Some callers cannot allocate device memory at the moment they extract a
-// mesh: code running inside a CUDA graph capture (where cudaMalloc is not
-// allowed), callbacks of a host framework that owns the whole device memory
-// pool, or real-time loops that must never block in the allocator.  This
-// entry point serves them.  The caller passes the volume, the output buffers
+// mesh: callbacks of a host framework that owns the whole device memory pool
+// (an allocation would compete with it), or real-time loops that must never
+// block in the allocator.  This entry point serves them.  The caller passes the volume, the output buffers
 // and a small counts buffer (device memory it already owns); every piece of
 // scratch the kernels need -- per-column counts and their scan, activity
 // bytes, look-back state, coordinate tables, the Marching Cubes active-cell
@@ -47,7 +46,9 @@ void *g_scratch_ptr[MAX_DEVICES];  // device address of g_scratch, per device
 std::mutex g_setup;
 
 // The device address of g_scratch on the current device; looked up once per
-// device (host code cannot use the symbol itself as an address).
+// device and kept for the process (host code cannot use the symbol itself as
+// an address).  A cudaDeviceReset loads the module again, possibly elsewhere:
+// the header tells callers not to use this entry point on a device after that.
 cudaError_t scratch_address(void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -1,8 +1,8 @@
 // Serving loop behind the C ABI (mesh_server_* in include/meshing_gb300.h).
 //
 // No counterpart in the reference, which answers one isosurface() call at a
-// time.  Requests (a device-resident volume, its shape and the algorithm
-// parameters) arrive on any thread and wait in a FIFO queue.  A loop thread
+// time.  Requests (a volume in device or host memory, its shape and the
+// algorithm parameters) arrive on any thread and wait in a FIFO queue.  A loop thread
 // admits them by continuous batching: whenever one of the server's wave slots
 // is free it takes queued requests in order while the device pool can reserve
 // each one's worst-case vertex / face output (and the wave's scratch), and
@@ -11,7 +11,14 @@
 //     batch (k_classify_batch .. k_expand_mc<EXP_BATCH>) that writes every
 //     volume's mesh straight into that request's own output block;
 //   * Marching Tetrahedra and Naive Surface Nets requests run the
-//     single-volume kernels on the slot's context, into their output blocks.
+//     single-volume kernels on the slot's context, into their output blocks;
+//   * welded Marching Cubes requests run the slot context's welded extraction
+//     (the Marching Cubes kernels, then the weld, in the context's own scratch)
+//     and their welded mesh is copied into their output blocks.
+// A host volume gets a block of the pool for itself at admission (counted
+// against the budget like the outputs), is uploaded on the slot's stream ahead
+// of its wave's kernels and gives the block back when the wave's results are
+// published.
 // Waves on different slots overlap on the device.  A host function queued
 // after the wave's kernels stamps the completion time, publishes the counts
 // and frees the wave's scratch; a request's output block stays reserved, and
@@ -136,7 +143,10 @@ enum { RQ_QUEUED = 0, RQ_RUNNING = 1, RQ_DONE = 2, RQ_FAILED = 3 };
 
 struct Req {
     int64_t id = 0;
-    const void *vol = nullptr;
+    const void *vol = nullptr;        // device volume (for a host request: its pool copy, once uploaded)
+    const void *host_vol = nullptr;   // host volume of a host request
+    size_t vol_bytes = 0;             // bytes of a host request's volume
+    Block vin;                        // its pool copy while the request is in flight
     int T = 0;
     int64_t dims[3] = {0, 0, 0};
     mesh_params p{};
@@ -291,13 +301,16 @@ void bounds(Req *r) {
     const bool cells = nx > 1 && ny > 1 && nz > 1;
     const int64_t nc = cells ? (nx - 1) * (ny - 1) * (nz - 1) : 0, nn = cells ? nx * ny * nz : 0;
     switch (r->p.alg) {
-    case MESH_ALG_MC: r->vcap = 12 * nc; r->fcap = 5 * nc; break;
+    case MESH_ALG_MC:
+    case MESH_ALG_MC_WELDED: r->vcap = 12 * nc; r->fcap = 5 * nc; break;
     case MESH_ALG_MT: r->vcap = 7 * nn; r->fcap = 12 * nc; break;
     default: r->vcap = nc; r->fcap = 6 * nn; break;
     }
     r->vbytes = up((size_t)r->vcap * 3 * (r->out64 ? 8 : 4));
 }
 size_t out_bytes(const Req &r) { return r.vbytes + up((size_t)r.fcap * 24); }
+// Pool bytes a request holds while in flight: outputs, and a host volume's copy.
+size_t held_bytes(const Req &r) { return out_bytes(r) + (r.host_vol ? up(r.vol_bytes) : 0); }
 
 struct GroupKey {
     int T, iso_type, range_type;
@@ -322,7 +335,7 @@ void form_wave(mesh_server *s, Slot &sl) {
     size_t reserved = 0;
     while (!s->queue.empty() && admitted < s->max_wave) {
         Req &r = s->reqs[s->queue.front()];
-        const size_t est = out_bytes(r) + (r.p.alg == MESH_ALG_MC ? vol_scratch_bytes(r) : 0);
+        const size_t est = held_bytes(r) + (r.p.alg == MESH_ALG_MC ? vol_scratch_bytes(r) : 0);
         if (admitted && reserved + est > share_cap) break;
         reserved += est;
         int gi = -1;
@@ -332,6 +345,10 @@ void form_wave(mesh_server *s, Slot &sl) {
             if (gi < 0 && (int)sl.groups.size() == MAX_GROUPS) break;
         }
         if (!s->pool.alloc(out_bytes(r), &r.out)) break;
+        if (r.host_vol && !s->pool.alloc(up(r.vol_bytes), &r.vin)) {
+            s->pool.release(&r.out);
+            break;
+        }
         if (r.p.alg == MESH_ALG_MC) {
             if (gi < 0) {
                 Group g;
@@ -357,6 +374,7 @@ void form_wave(mesh_server *s, Slot &sl) {
                 grp.bound -= share;
                 if (grp.reqs.empty()) sl.groups.erase(sl.groups.begin() + gi);
                 s->pool.release(&r.out);
+                s->pool.release(&r.vin);
                 break;
             }
         } else {
@@ -376,6 +394,7 @@ void form_wave(mesh_server *s, Slot &sl) {
         for (auto it = sl.groups[g].reqs.rbegin(); it != sl.groups[g].reqs.rend(); ++it) {
             Req &r = s->reqs[*it];
             s->pool.release(&r.out);
+            s->pool.release(&r.vin);
             r.state = RQ_QUEUED;
             s->queue.push_front(*it);
             sl.wave.erase(*it);
@@ -392,6 +411,7 @@ void fail_wave(mesh_server *s, Slot &sl, int rc) {
             Req &r = s->reqs[id];
             r.state = RQ_FAILED;
             r.status = rc;
+            s->pool.release(&r.vin);
             s->failed++;
         }
         s->pool.release(&g.scratch);
@@ -400,6 +420,7 @@ void fail_wave(mesh_server *s, Slot &sl, int rc) {
         Req &r = s->reqs[id];
         r.state = RQ_FAILED;
         r.status = rc;
+        s->pool.release(&r.vin);
         s->failed++;
     }
     sl.groups.clear();
@@ -454,6 +475,7 @@ void CUDART_CB wave_done(void *arg) {
     size_t room = 0;  // the largest worst case of the wave
     auto record = [&](Req &r, int64_t nv, int64_t nf, unsigned err) {
         room = std::max(room, r.out.size);
+        s->pool.release(&r.vin);  // the wave's kernels are done with a host volume's copy
         if (err) {  // the worst-case block stays reserved until the release
             r.status = (err & ERR_CAPACITY) ? MESH_ECAPACITY : MESH_EDEVICE;
             return;
@@ -481,7 +503,7 @@ void CUDART_CB wave_done(void *arg) {
     }
     if (!s->queue.empty()) {
         const Req &h = s->reqs[s->queue.front()];
-        room = std::max(room, out_bytes(h) + (h.p.alg == MESH_ALG_MC ? vol_scratch_bytes(h) : 0));
+        room = std::max(room, held_bytes(h) + (h.p.alg == MESH_ALG_MC ? vol_scratch_bytes(h) : 0));
     }
     if (s->pool.largest() < room) {
         sl->finishing = 1;
@@ -594,6 +616,16 @@ int launch_wave(mesh_server *s, Slot &sl) {
         sl.res_cap = cap / 8;
         memset(sl.res, 0, words * 8 + 8);  // error words are copied into their low halves
     }
+    // host volumes go up first, into their pool blocks; the wave reads those
+    for (auto &kv : sl.wave) {
+        Req &r = kv.second;
+        if (!r.host_vol) continue;
+        if (r.vol_bytes &&
+            (e = cudaMemcpyAsync(s->arena + r.vin.off, r.host_vol, r.vol_bytes, cudaMemcpyHostToDevice, sl.stream)) !=
+                cudaSuccess)
+            return MESH_ECUDA;
+        r.vol = s->arena + r.vin.off;
+    }
     // exact layouts; every batch gets its own region of the pinned staging
     std::vector<GroupLayout> lays(sl.groups.size());
     size_t stage = 0;
@@ -702,6 +734,21 @@ int launch_wave(mesh_server *s, Slot &sl) {
         if ((e = cudaMemsetAsync(sl.d_counts, 0, need, sl.stream)) != cudaSuccess) return MESH_ECUDA;
         for (size_t i = 0; i < sl.singles.size(); i++) {
             const Req &r = sl.wave.at(sl.singles[i]);
+            if (r.p.alg == MESH_ALG_MC_WELDED) {
+                // the context's welded extraction (it waits for the slot's stream),
+                // then a device copy of the welded mesh into the output block
+                int64_t cnt[3] = {0, 0, 0};
+                int rc = mesh_count(sl.ctx, r.vol, r.T, r.dims[0], r.dims[1], r.dims[2], 1, &r.p, &cnt[0], &cnt[1]);
+                if (rc == MESH_OK && (cnt[0] > r.vcap || cnt[1] > r.fcap)) rc = MESH_ECAPACITY;
+                if (rc == MESH_OK)
+                    rc = mesh_fill(sl.ctx, s->arena + r.out.off, (int64_t *)(s->arena + r.out.off + r.vbytes), 1);
+                if (rc) return rc;
+                // (a pageable source: the copy takes the values before it returns)
+                if ((e = cudaMemcpyAsync(sl.d_counts + 3 * i, cnt, sizeof(cnt), cudaMemcpyHostToDevice, sl.stream)) !=
+                    cudaSuccess)
+                    return MESH_ECUDA;
+                continue;
+            }
             int rc = mesh_extract_device(sl.ctx, r.vol, r.T, r.dims[0], r.dims[1], r.dims[2], &r.p,
                                          s->arena + r.out.off, r.vcap, (int64_t *)(s->arena + r.out.off + r.vbytes),
                                          r.fcap, sl.d_counts + 3 * i);
@@ -853,15 +900,19 @@ void mesh_server_destroy(mesh_server *s) {
 const char *mesh_server_last_error(const mesh_server *s) { return s ? s->msg.c_str() : ""; }
 
 int mesh_server_submit(mesh_server *s, const void *vol, int vol_dtype, int64_t nx, int64_t ny, int64_t nz,
-                       const mesh_params *p, int64_t *id) {
+                       int vol_on_device, const mesh_params *p, int64_t *id) {
     if (!s || !p || !id) return MESH_EINVAL;
     *id = 0;
     int rc = validate(nullptr, vol_dtype, nx, ny, nz, p);
     if (rc) return sfail(s, rc, "invalid request");
-    if (p->alg == MESH_ALG_MC_WELDED) return sfail(s, MESH_EINVAL, "welded meshes are not served");
     if (!vol && nx > 1 && ny > 1 && nz > 1) return sfail(s, MESH_EINVAL, "volume is NULL");
     Req r;
-    r.vol = vol;
+    if (vol_on_device) {
+        r.vol = vol;
+    } else if (nx > 1 && ny > 1 && nz > 1) {
+        r.host_vol = vol;
+        r.vol_bytes = (size_t)nx * ny * nz * dtype_size(vol_dtype);
+    }
     r.T = vol_dtype;
     r.dims[0] = nx; r.dims[1] = ny; r.dims[2] = nz;
     r.p = *p;
@@ -874,8 +925,8 @@ int mesh_server_submit(mesh_server *s, const void *vol, int vol_dtype, int64_t n
         s->have_t0 = true;
         s->t0 = clk::now();
     }
-    // the worst case alone (with its batch scratch) must fit the whole pool
-    size_t need = out_bytes(r);
+    // the worst case alone (with its batch scratch and a host volume's copy) must fit the whole pool
+    size_t need = held_bytes(r);
     if (r.p.alg == MESH_ALG_MC) need += GROUP_FIXED_BYTES + vol_scratch_bytes(r);
     if (need > s->pool.cap) {
         s->rejected++;
@@ -927,7 +978,7 @@ int mesh_server_release(mesh_server *s, int64_t id) {
     if (it->second.state == RQ_QUEUED || it->second.state == RQ_RUNNING)
         return sfail(s, MESH_ESTATE, "request still in flight");
     for (Block *b : {&it->second.out, &it->second.keep_v, &it->second.keep_f, &it->second.move_v,
-                     &it->second.move_f})
+                     &it->second.move_f, &it->second.vin})
         s->pool.release(b);
     s->reqs.erase(it);
     s->cv.notify_all();
@@ -1002,7 +1053,7 @@ int mesh_server_replay(mesh_server *s, int n, const void *const *vols, const int
             if (left > std::chrono::microseconds(300)) std::this_thread::sleep_for(left - std::chrono::microseconds(200));
         }
         int64_t id = 0;
-        const int rc = mesh_server_submit(s, vols[i], dtypes[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2],
+        const int rc = mesh_server_submit(s, vols[i], dtypes[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], 1,
                                           &params[i], &id);
         std::lock_guard<std::mutex> lk(m);
         ids.push_back(rc == MESH_OK ? id : -1);

@@ -1,6 +1,7 @@
 """Serving loop: continuous batching of isosurface requests (mesh_server_*).
 
-Each request names a CUDA volume and an algorithm; the server answers with
+Each request names a volume (a CUDA tensor, or a host array the server uploads
+into its pool) and an algorithm; the server answers with
 exactly the mesh ``isosurface(A, method, X, Y, Z)`` returns for it alone, kept
 resident on the device until released.
 
@@ -15,10 +16,18 @@ import numpy as np
 
 from . import _lib
 from ._lib import MESH_DT_F32, MESH_DT_F64, MESH_DT_U16, MeshError
-from .api import MarchingCubes, _torch_julia_layout, make_params
+from .api import _VOL_DT, MarchingCubes, _torch_julia_layout, make_params
 from .batch import _DeviceArray
 
 STATE = {0: 'queued', 1: 'running', 2: 'done', 3: 'failed'}
+
+
+def _is_cuda_tensor(A):
+    try:
+        import torch
+    except ImportError:
+        return False
+    return isinstance(A, torch.Tensor) and A.is_cuda
 
 
 class Server:
@@ -54,21 +63,33 @@ class Server:
             pass
 
     def submit(self, A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1)):
-        """Queue isosurface(A, method, X, Y, Z) for CUDA volume A; returns the request id."""
-        import torch
+        """Queue isosurface(A, method, X, Y, Z); returns the request id.
+
+        A: a 3-D CUDA tensor (read in place), or a numpy array / CPU tensor
+        indexed [x, y, z], which the server uploads into its pool when the
+        request is admitted (kept referenced here until the request is released)."""
         method = method or MarchingCubes()
-        dt = _lib.torch_dtype_code(A.dtype)
-        if dt is None or A.dim() != 3 or not A.is_cuda:
-            raise TypeError('volume must be a 3-D CUDA tensor of UInt16, Int32, Int64, Float32 or Float64')
-        t = _torch_julia_layout(A)
         p = make_params(method, X, Y, Z)
+        if _is_cuda_tensor(A):
+            import torch
+            dt = _lib.torch_dtype_code(A.dtype)
+            if dt is None or A.dim() != 3:
+                raise TypeError('volume must be a 3-D tensor of a supported eltype')
+            t = _torch_julia_layout(A)
+            # the server reads the volume on its own streams: finish writing it first
+            torch.cuda.current_stream(t.device).synchronize()
+            ptr, shape, on_device = t.data_ptr(), tuple(t.shape), 1
+        else:
+            t = np.asfortranarray(A.numpy() if hasattr(A, 'numpy') else np.asarray(A))
+            dt = _VOL_DT.get(t.dtype)
+            if dt is None or t.ndim != 3:
+                raise TypeError('volume must be a 3-D array of a supported eltype')
+            ptr, shape, on_device = t.ctypes.data, t.shape, 0
         bits = ctypes.c_int()
         self._check(self._lib.mesh_output_float_bits(dt, ctypes.byref(p), ctypes.byref(bits)))
-        # the server reads the volume on its own streams: finish writing it first
-        torch.cuda.current_stream(t.device).synchronize()
         rid = ctypes.c_int64()
-        nx, ny, nz = t.shape
-        self._check(self._lib.mesh_server_submit(self.handle, ctypes.c_void_p(t.data_ptr()), dt, nx, ny, nz,
+        nx, ny, nz = shape
+        self._check(self._lib.mesh_server_submit(self.handle, ctypes.c_void_p(ptr), dt, nx, ny, nz, on_device,
                                                  ctypes.byref(p), ctypes.byref(rid)))
         self._live[rid.value] = (t, bits.value)
         return rid.value

@@ -2,8 +2,9 @@
 
 Every request must give exactly the mesh isosurface() gives for it alone,
 whether it ran alone or in a wave with others (Marching Cubes requests of a
-wave share one batch; waves overlap on the device); admission respects the
-memory budget and the queue limit.
+wave share one batch; waves overlap on the device), from a device or a host
+volume, welded or not; admission respects the memory budget and the queue
+limit.
 """
 import numpy as np
 import pytest
@@ -156,12 +157,65 @@ def test_small_int_and_float16_requests(pkg, cuda):
     srv = pkg.Server(budget_bytes=2 << 30)
     for A, iso in vols:
         for m in (pkg.MarchingCubes(iso=iso), pkg.MarchingTetrahedra(iso=iso, eps=np.float32(1e-3)),
-                  pkg.NaiveSurfaceNets(iso=iso)):
+                  pkg.NaiveSurfaceNets(iso=iso), pkg.MarchingCubes(iso=iso, weld=True)):
             want = pkg.isosurface(A, m)
             rid = srv.submit(A, m)
             assert same(torch, srv.result(rid), want), (A.dtype, type(m).__name__)
             srv.release(rid)
-    with pytest.raises(pkg.MeshError):
-        srv.submit(vols[0][0], pkg.MarchingCubes(iso=np.float32(0.5), weld=True))
     srv.close()
     del rng
+
+
+def test_host_volumes_and_welded_requests_alone_and_in_the_mix(pkg, cuda):
+    # requests whose volumes are host arrays (uploaded into the pool at
+    # admission) and welded Marching Cubes requests, mixed with device
+    # requests: every result equals the request's own isosurface call, in the
+    # mix and alone, and the host volumes' pool blocks are returned
+    torch = cuda
+    reqs = requests(torch, pkg, 40, 5)
+    mixed = []
+    for i, (A, m, r) in enumerate(reqs):
+        if i % 3 == 0:
+            A = A.cpu().numpy()                           # host volume
+        if i % 4 == 1 and type(m).__name__ == 'MarchingCubes':
+            m = pkg.MarchingCubes(iso=m.iso, weld=True)   # welded
+        mixed.append((A, m, r))
+    want = [pkg.isosurface(torch.from_numpy(A).cuda() if isinstance(A, np.ndarray) else A, m, *r)
+            for A, m, r in mixed]
+    assert any(isinstance(A, np.ndarray) for A, _, _ in mixed) and any(getattr(m, 'weld', False) for _, m, _ in mixed)
+    srv = pkg.Server(budget_bytes=6 << 30, slots=3, max_wave=16)
+    ids = [srv.submit(A, m, *r) for A, m, r in mixed]
+    for i, rid in enumerate(ids):
+        got = srv.result(rid)
+        assert same(torch, got, want[i]), i
+        srv.release(rid)
+    st = srv.stats()
+    assert st['completed'] == len(mixed) and st['failed'] == 0
+    assert st['reserved_bytes'] == 0                      # host volumes' copies given back
+    for i, (A, m, r) in enumerate(mixed[:9]):
+        rid = srv.submit(A, m, *r)
+        assert same(torch, srv.result(rid), want[i]), i
+        srv.release(rid)
+    srv.close()
+
+
+def test_host_volume_bytes_count_against_the_budget(pkg, cuda):
+    # a host request's worst case includes its volume's pool copy: a budget that
+    # holds the outputs of a device request but not the volume beside them
+    # rejects the same request from host memory
+    torch = cuda
+    A = torch.rand((64, 64, 64), device='cuda', dtype=torch.float64)
+    m = pkg.NaiveSurfaceNets(iso=0.5)
+    probe = pkg.Server(budget_bytes=1 << 30)
+    rid = probe.submit(A, m)
+    probe.wait(rid)
+    W = int(probe.stats()['peak_reserved_bytes'])   # outputs of the device request
+    probe.close()
+    srv = pkg.Server(budget_bytes=W + (64 ** 3 * 8) // 2)
+    rid = srv.submit(A, m)
+    srv.result(rid)
+    srv.release(rid)
+    with pytest.raises(pkg.MeshError) as ei:
+        srv.submit(A.cpu().numpy(), m)
+    assert ei.value.status == 9  # MESH_EBUDGET
+    srv.close()

@@ -1,14 +1,15 @@
 """mesh_extract_noalloc: extraction for callers that cannot allocate.
 
-Code inside CUDA graph capture, callbacks of a framework that owns the device
-memory pool, and real-time loops cannot call cudaMalloc when they extract a
-mesh.  mesh_extract_noalloc keeps its scratch in a static device array of
-MESH_NOALLOC_SCRATCH_BYTES instead.  These tests call it through the C ABI
-and check that it returns exactly what the allocating entry point
-mesh_extract_device returns (the same contract as every parity test:
+Callbacks of a framework that owns the whole device memory pool, and
+real-time loops that must never block in an allocator, cannot call cudaMalloc
+when they extract a mesh.  mesh_extract_noalloc keeps its scratch in a static
+device array of MESH_NOALLOC_SCRATCH_BYTES instead.  These tests call it
+through the C ABI and check that it returns exactly what the allocating entry
+point mesh_extract_device returns (the same contract as every parity test:
 connectivity and counts bit-exact, positions within 1e-12 / 2 ulp -- here
 bit-identical), on calls made back to back so that the second call runs on
-the scratch the first one left behind.
+the scratch the first one left behind, and, per algorithm, exactly the
+oracle's mesh.
 """
 import ctypes
 
@@ -119,3 +120,32 @@ def test_noalloc_rejects_calls_beyond_its_scratch(pkg, cuda):
                                   ctypes.c_void_p(counts.data_ptr()), None)
     assert rc == 8  # MESH_ESCRATCH
     assert lib.mesh_status_string(8) == b'needs more scratch than the no-allocation limit'
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_noalloc_matches_the_oracle(pkg, oracle, cuda, alg):
+    # one whole z segment per column (the tiling this entry point uses) against
+    # the CPU oracle, bit for bit
+    torch = cuda
+    vol = _volume(torch, (45, 38, 70), 'waves', torch.float32)
+    A = np.asfortranarray(vol.cpu().numpy())
+    iso, ranges = np.float32(0.05), ((0.0, 1.0), (-1.0, 1.0), (0.0, 2.0))
+    method = {'mc': pkg.MarchingCubes(iso=iso), 'mt': pkg.MarchingTetrahedra(iso=iso, eps=1e-3),
+              'nsn': pkg.NaiveSurfaceNets(iso=iso)}[alg]
+    wv, wf = oracle.isosurface(A, alg, iso, 1e-3, ranges)
+    ft = torch.float32 if wv.dtype == np.float32 else torch.float64
+    verts = torch.empty((len(wv), 3), dtype=ft, device='cuda')
+    faces = torch.empty((len(wf), 3), dtype=torch.int64, device='cuda')
+    counts = torch.full((3,), -1, dtype=torch.int64, device='cuda')
+    p = pkg.make_params(method, *ranges)
+    lib = pkg.load_library()
+    for _ in range(2):  # twice in a row on the same scratch
+        rc = lib.mesh_extract_noalloc(ctypes.c_void_p(vol.data_ptr()), 2, *vol.shape, ctypes.byref(p),
+                                      ctypes.c_void_p(verts.data_ptr()), len(wv), ctypes.c_void_p(faces.data_ptr()),
+                                      len(wf), ctypes.c_void_p(counts.data_ptr()),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert counts.tolist() == [len(wv), len(wf), 0]
+        assert np.array_equal(faces.cpu().numpy(), wf)
+        assert np.array_equal(verts.cpu().numpy().view(np.uint8), wv.view(np.uint8))
