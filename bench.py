@@ -467,11 +467,14 @@ def run_ours(args, rank, world, dist):
         'e2e': {'value': whole_job_rate(vox, world, e2e_ms) / 1e9, 'unit': 'Gvoxels/s', 'ms_per_step': e2e_ms,
                 'h2d_bytes_per_step': int(in_b), 'd2h_bytes_per_step': int(out_b),
                 'count_ms': _spread([c for c, _ in split]), 'fill_ms': _spread([f for _, f in split]),
+                'step_ms': _spread([c + f for c, f in split]),
                 'link': link, 'link_bound_ms': (in_b / link['h2d_gbs'] + out_b / link['d2h_gbs']) / 1e6},
         'gpu_launches': int(sum(v[1] for v in st.values())),
         'cpu_baseline': cpu,
         'clocks': ck,
     }
+    e = line['e2e']
+    e['median_over_link_bound'] = e['step_ms']['median'] / e['link_bound_ms']
     line.update(extras)
     print(json.dumps(line), flush=True)
 

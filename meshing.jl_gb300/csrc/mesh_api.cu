@@ -254,6 +254,13 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     const int64_t target = (int64_t)c->sms * 64;
     const int maxseg = (P.cz + ZC - 1) / ZC;
     int nseg = (int)std::min<int64_t>(maxseg, std::max<int64_t>(1, (target + per_seg - 1) / per_seg));
+    // a host volume uploaded in groups of z segments (upload_and_classify) gets at
+    // least PIPE_MAX segments, so that all but the last group's classification
+    // runs under the upload (a mapped host volume read in place is not uploaded)
+    const size_t vbytes0 = (size_t)nx * ny * nz * dtype_size(T);
+    if (!vol_on_device && !c->zerocopy && c->pipe_bytes > 0 && (int64_t)vbytes0 >= c->pipe_bytes && !c->want_tma &&
+        !c->one_walk)
+        nseg = std::min(maxseg, std::max(nseg, PIPE_MAX));
     int zs = (P.cz + nseg - 1) / nseg;
     zs = (zs + ZC - 1) / ZC * ZC;
     P.zs = zs;
