@@ -102,13 +102,21 @@ MESH_API void mesh_ctx_destroy(mesh_ctx *ctx);
    mesh_fill downloads a Marching Cubes mesh in x ranges while the next range is emitted.
    Both calls still return only when their work is complete. */
 MESH_API int mesh_ctx_set_stream(mesh_ctx *ctx, void *stream);
-/* No counterpart in the reference.  Until reset with (0, 0), the volumes of the
- * context's calls are x samples x_first .. x_first+nx-1 of a volume whose x axis
- * has nx_total samples: node coordinates are those of LinRange(first(X),
- * last(X), nx_total), so a Marching Cubes x slab meshes exactly as that part of
- * the whole volume (x is the outermost emission axis: slab meshes concatenate
- * into the whole one, face indices offset by the vertices before them). */
-MESH_API int mesh_set_x_window(mesh_ctx *ctx, int64_t x_first, int64_t nx_total);
+/* No counterpart in the reference.  Until reset with (0, 0, 0), the volumes of
+ * the context's calls are x samples x_first .. x_first+nx-1 of a volume whose x
+ * axis has nx_total samples: node coordinates are those of LinRange(first(X),
+ * last(X), nx_total), so an x slab meshes exactly as that part of the whole
+ * volume (x is the outermost emission axis: slab meshes concatenate into the
+ * whole one, face indices offset by the vertices before them).  Marching Cubes
+ * slabs of cells [c0, c1) pass samples c0 .. c1 with halo = 0.  Marching
+ * Tetrahedra and Naive Surface Nets share vertices across the boundary, which
+ * belong to the lower cell column: every slab after the first passes samples
+ * c0-1 .. c1 with x_first = c0-1 and halo = 1; its first cell column (the
+ * previous slab's last) is counted but not emitted, mesh_count returns the
+ * counts without it, and faces that use the previous slab's vertices have
+ * indices <= 0 before the offset is added.  With halo = 1, mesh_extract_device
+ * returns MESH_EINVAL, and so does a Marching Cubes call. */
+MESH_API int mesh_set_x_window(mesh_ctx *ctx, int64_t x_first, int64_t nx_total, int halo);
 MESH_API const char *mesh_status_string(int status);
 /* Last error message recorded on `ctx` (empty string if none). */
 MESH_API const char *mesh_ctx_last_error(const mesh_ctx *ctx);

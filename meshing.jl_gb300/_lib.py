@@ -58,7 +58,7 @@ def load():
         'mesh_ctx_create': (c_int, [c_int, P(vp)]),
         'mesh_ctx_destroy': (None, [vp]),
         'mesh_ctx_set_stream': (c_int, [vp, vp]),
-        'mesh_set_x_window': (c_int, [vp, ctypes.c_int64, ctypes.c_int64]),
+        'mesh_set_x_window': (c_int, [vp, ctypes.c_int64, ctypes.c_int64, c_int]),
         'mesh_vertex_normals': (c_int, [vp, vp, c_int, ctypes.c_int64, vp, ctypes.c_int64, vp]),
         'mesh_status_string': (ctypes.c_char_p, [c_int]),
         'mesh_ctx_last_error': (ctypes.c_char_p, [vp]),

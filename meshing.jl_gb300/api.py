@@ -231,22 +231,28 @@ def isosurface(A, *args, ctx=None):
 
 def isosurface_slabs(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), slab_cells=None, slab_bytes=4 << 30,
                      ctx=None):
-    """Marching Cubes of a host volume larger than device memory, one x slab at a time.
+    """isosurface of a host volume larger than device memory, one x slab at a time.
 
     x is the outermost axis of the reference's emission order
-    (src/marching_cubes.jl:40), so the meshes of consecutive x slabs of cells,
-    concatenated with face indices offset by the vertices before them, are the
-    mesh of the whole volume.  Slab k holds cells [c0, c1) and samples
-    [c0, c1]; its node coordinates are those of the whole volume's LinRange
-    (mesh_set_x_window).  ``A`` is a numpy array (or memmap) indexed [x, y, z];
-    ``slab_cells`` cells per slab, or as many as fit ``slab_bytes`` of volume.
-    Returns numpy (points, faces) equal to ``isosurface(A, method, X, Y, Z)``.
-    MarchingTetrahedra and NaiveSurfaceNets share vertices between cells on
-    both sides of a slab boundary, so they are not split.
+    (src/marching_cubes.jl:40, src/marching_tetrahedra.jl:144), so the meshes of
+    consecutive x slabs of cells, concatenated with face indices offset by the
+    vertices before them, are the mesh of the whole volume.  Slab k holds cells
+    [c0, c1); its node coordinates are those of the whole volume's LinRange
+    (mesh_set_x_window).  Marching Cubes slabs read samples [c0, c1].
+    MarchingTetrahedra and NaiveSurfaceNets share vertices between cells: a
+    vertex on a slab boundary belongs to the cell column before it (the first
+    cell to touch an edge is the lowest one), so every slab after the first
+    reads samples [c0 - 1, c1] -- the previous slab's last cell column is its
+    halo, counted but not emitted -- and its faces that use the previous slab's
+    vertices come back with indices <= 0 before the offset is added.
+    ``A`` is a numpy array (or memmap) indexed [x, y, z]; ``slab_cells`` cells
+    per slab, or as many as fit ``slab_bytes`` of volume.  Returns numpy
+    (points, faces) equal to ``isosurface(A, method, X, Y, Z)``.
     """
     method = method or MarchingCubes()
-    if not isinstance(method, MarchingCubes) or method.weld:
-        raise TypeError('only (unwelded) MarchingCubes meshes split into x slabs')
+    if getattr(method, 'weld', False):
+        raise TypeError('welded meshes do not split into x slabs')
+    halo = not isinstance(method, MarchingCubes)
     p = make_params(method, X, Y, Z)
     dt = _VOL_DT.get(np.dtype(A.dtype))
     if dt is None or A.ndim != 3:
@@ -258,15 +264,17 @@ def isosurface_slabs(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), slab_cells
     ft = np.float32 if bits.value == 32 else np.float64
     if slab_cells is None:
         plane = ny * nz * A.dtype.itemsize
-        slab_cells = max(1, int(slab_bytes // max(plane, 1)) - 1)
+        slab_cells = max(1, int(slab_bytes // max(plane, 1)) - 1 - (1 if halo else 0))
     c = ctx or default_context(0)
     c.set_stream(None)
     vs, fs, voff = [], [], 0
     try:
         for c0 in range(0, max(nx - 1, 0), slab_cells):
             c1 = min(c0 + slab_cells, nx - 1)
-            S = np.asfortranarray(A[c0:c1 + 1])
-            check(lib.mesh_set_x_window(c.handle, c0, nx), c.handle)
+            h = 1 if (halo and c0 > 0) else 0
+            s0 = c0 - h   # first sample (the halo column's, after slab 0)
+            S = np.asfortranarray(A[s0:c1 + 1])
+            check(lib.mesh_set_x_window(c.handle, s0, nx, h), c.handle)
             nv, nf = ctypes.c_int64(), ctypes.c_int64()
             check(lib.mesh_count(c.handle, ctypes.c_void_p(S.ctypes.data), dt, S.shape[0], ny, nz, 0,
                                  ctypes.byref(p), ctypes.byref(nv), ctypes.byref(nf)), c.handle)
@@ -279,7 +287,7 @@ def isosurface_slabs(A, method=None, X=(-1, 1), Y=(-1, 1), Z=(-1, 1), slab_cells
             vs.append(v)
             fs.append(f)
     finally:
-        lib.mesh_set_x_window(c.handle, 0, 0)
+        lib.mesh_set_x_window(c.handle, 0, 0, 0)
     if not vs:
         return np.empty((0, 3), dtype=ft), np.empty((0, 3), dtype=np.int64)
     return np.concatenate(vs), np.concatenate(fs)

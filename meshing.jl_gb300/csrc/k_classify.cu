@@ -89,13 +89,13 @@ __device__ __forceinline__ void step(const Plan &p, const uint32_t *s_tab, const
             c.f[r] += t >> 8;
         } else if (ALG == MESH_ALG_MT) {
             const uint32_t t = s_tab[mt_case(a, b, cc, d)];
-            const int bnd = (xs == 0) | ((y0 + r == 0) << 1) | ((zc == 0) << 2);
+            const int bnd = (xs + p.xg0 == 0) | ((y0 + r == 0) << 1) | ((zc == 0) << 2);
             c.v[r] += __popc(t & p.own[bnd] & 0x7ffffu);
             c.f[r] += t >> 24;
         } else {  // NSN: one vertex per active cell, a quad per crossed base edge
             c.v[r] += 1;
             const unsigned s0 = cm & 1u;
-            const bool yk = y0 + r > 0, zk = zc > 0, xk = xs > 0;
+            const bool yk = y0 + r > 0, zk = zc > 0, xk = xs + p.xg0 > 0;
             unsigned q = 0;
             q += (s0 != ((cm >> 1) & 1u)) && yk && zk;  // +x edge
             q += (s0 != ((cm >> 3) & 1u)) && zk && xk;  // +y edge

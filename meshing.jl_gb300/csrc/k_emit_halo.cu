@@ -160,6 +160,12 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
     const T *vol = (const T *)p.vol;
     const int64_t sxy = p.nx * p.ny;
     const int64_t np = p.pstride;
+    // with an x halo, the totals of its cell column (every output is shifted by them)
+    int64_t V0 = 0, F0 = 0;
+    if (p.xhalo && p.cx > 1) {
+        V0 = p.base[piece(p, 0, 0, 1)];
+        F0 = p.base[np + piece(p, 0, 0, 1)];
+    }
 
     bool rowok[R + 1];
     const T *rowp[R + 1];
@@ -208,14 +214,14 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
         const int yc = y0 - 1 + r;
         if (ALG == MESH_ALG_MT) {
             cs = mt_case(a, b, c, d);
-            const int bnd = (xs == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
+            const int bnd = (xs + p.xg0 == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
             nv = __popc(tb->touched[cs] & p.own[bnd] & 0x7ffffu);
             nf = tb->nfaces[cs];
         } else {
             cs = cm;
             nv = 1;
             const unsigned s0 = cm & 1u;
-            const bool xk = xs > 0, yk = yc > 0, zk = zc > 0;
+            const bool xk = xs + p.xg0 > 0, yk = yc > 0, zk = zc > 0;
             nf = 2 * (int)(((s0 != ((cm >> 1) & 1u)) && yk && zk) + ((s0 != ((cm >> 3) & 1u)) && zk && xk) +
                            ((s0 != ((cm >> 4) & 1u)) && xk && yk));
         }
@@ -286,8 +292,8 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
 #pragma unroll
                 for (int r = 0; r < R; r++) {
                     int tv = 0, tf = 0;
-                    if (r >= 1 && realx && cs[r] != 0u) {
-                        if (bv[r] + nvs[r] > p.verts_cap || bf[r] + nfs[r] > p.faces_cap) {
+                    if (r >= 1 && realx && cs[r] != 0u && !(p.xhalo && xs == 0)) {
+                        if (bv[r] - V0 + nvs[r] > p.verts_cap || bf[r] - F0 + nfs[r] > p.faces_cap) {
                             atomicOr(p.err, ERR_CAPACITY);
                         } else {
                             tv = nvs[r];
@@ -316,10 +322,10 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                     const int k = t - (sc ? (int)ws.pv[sc - 1] : 0);
                     const unsigned c = ws.cas[cur][r][l];
                     const int xc = x0 + l, yc = y0 - 1 + r;
-                    const int64_t vb = ws.base[cur][r][l];
+                    const int64_t vb = ws.base[cur][r][l] - V0;  // this volume's first emitted vertex is 0
                     P q[3];
                     if (ALG == MESH_ALG_MT) {
-                        const int bnd = (xc == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
+                        const int bnd = (xc + p.xg0 == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
                         const uint32_t own = p.own[bnd];
                         // the k-th owned edge in the cell's first-use order
                         const int nt = __popc(tb->touched[c]);
@@ -376,10 +382,10 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                     const int f = t - (sc ? (int)ws.pf[sc - 1] : 0);
                     const unsigned c = ws.cas[cur][r][l];
                     const int xc = x0 + l, yc = y0 - 1 + r;
-                    const int64_t vb = ws.base[cur][r][l];
-                    int64_t *o = p.faces + 3 * (ws.fbase[r][l] + f);
+                    const int64_t vb = ws.base[cur][r][l] - V0;
+                    int64_t *o = p.faces + 3 * (ws.fbase[r][l] - F0 + f);
                     if (ALG == MESH_ALG_MT) {
-                        const int bnd = (xc == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
+                        const int bnd = (xc + p.xg0 == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
                         const uint32_t own = p.own[bnd];
                         int64_t id[3];
 #pragma unroll
@@ -394,8 +400,8 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                                 const int l2 = l - (sh & 1), r2 = r - ((sh >> 1) & 1);
                                 const int b2 = (sh & 4) ? (cur ^ 1) : cur;
                                 const unsigned c2 = ws.cas[b2][r2][l2];
-                                const int64_t base2 = ws.base[b2][r2][l2];
-                                const int bnd2 = ((xc - (sh & 1)) == 0) | (((yc - ((sh >> 1) & 1)) == 0) << 1) |
+                                const int64_t base2 = ws.base[b2][r2][l2] - V0;
+                                const int bnd2 = ((xc - (sh & 1) + p.xg0) == 0) | (((yc - ((sh >> 1) & 1)) == 0) << 1) |
                                                  (((zc - ((sh >> 2) & 1)) == 0) << 2);
                                 id[j] = base2 + __popc(tb->before[c2][e2] & p.own[bnd2]) + 1;
                             }
@@ -404,7 +410,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                     } else {
                         // NSN: the (f/2)-th crossed base edge of the cell, triangle f%2
                         const unsigned s0 = c & 1u;
-                        const bool xk = xc > 0, yk = yc > 0, zk = zc > 0;
+                        const bool xk = xc + p.xg0 > 0, yk = yc > 0, zk = zc > 0;
                         const bool ex[3] = {s0 != ((c >> 1) & 1u) && yk && zk, s0 != ((c >> 3) & 1u) && zk && xk,
                                             s0 != ((c >> 4) & 1u) && xk && yk};
                         int kind = 0;
@@ -425,7 +431,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                             Aa = ws.base[cur][r - 1][l - 1]; B = ws.base[cur][r - 1][l]; D = ws.base[cur][r][l - 1];
                         }
                         const int64_t C = vb + 1;
-                        Aa += 1; B += 1; D += 1;
+                        Aa += 1 - V0; B += 1 - V0; D += 1 - V0;
                         if (s0) {
                             if (f & 1) { o[0] = Aa; o[1] = C; o[2] = D; }
                             else { o[0] = Aa; o[1] = B; o[2] = C; }

@@ -246,6 +246,13 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     // welded Marching Cubes runs the Marching Cubes kernels, then welds
     c->weld = p->alg == MESH_ALG_MC_WELDED;
     if (c->weld) P.alg = MESH_ALG_MC;
+    // x window: MT / NSN take the grid-boundary rules at the whole volume's x = 0; with
+    // a halo, the volume's first cell column is the previous slab's last (counted, not
+    // emitted)
+    P.xg0 = c->win_nx ? c->win_x0 : 0;
+    P.xhalo = c->win_nx && c->win_halo;
+    if (P.xhalo && P.alg != MESH_ALG_MT && P.alg != MESH_ALG_NSN)
+        return fail(c, MESH_EINVAL, "a halo column is for MarchingTetrahedra / NaiveSurfaceNets slabs");
 
     // tiling
     P.tiles_x = (P.cx + TILE_X - 1) / TILE_X;
@@ -703,12 +710,14 @@ int mesh_ctx_set_stream(mesh_ctx *c, void *stream) {
     return MESH_OK;
 }
 
-int mesh_set_x_window(mesh_ctx *c, int64_t x_first, int64_t nx_total) {
+int mesh_set_x_window(mesh_ctx *c, int64_t x_first, int64_t nx_total, int halo) {
     if (!c) return MESH_EINVAL;
-    if (x_first < 0 || nx_total < 0 || (nx_total == 0 && x_first != 0) || nx_total > ((int64_t)1 << POS_BITS))
+    if (x_first < 0 || nx_total < 0 || (nx_total == 0 && (x_first != 0 || halo)) ||
+        nx_total > ((int64_t)1 << POS_BITS) || (halo != 0 && halo != 1))
         return fail(c, MESH_EINVAL, "invalid x window");
     c->win_x0 = x_first;
     c->win_nx = nx_total;
+    c->win_halo = halo;
     c->have_plan = 0;
     return MESH_OK;
 }
@@ -761,6 +770,38 @@ int run_weld(mesh_ctx *c) {
     return MESH_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// An x window with a halo column (MT / NSN slab after the first): the halo
+// column's vertices and faces come first in the scan and are not emitted, so
+// the counts lose its totals (the scanned base of piece (seg 0, y 0, x 1)).
+int drop_halo_counts(mesh_ctx *c) {
+    const Plan &P = c->plan;
+    int64_t v0 = c->nverts, f0 = c->nfaces;  // a window of the halo column alone emits nothing
+    if (P.cx > 1) {
+        GatherIdx gi{};
+        gi.n = 2;
+        gi.idx[0] = piece(P, 0, 0, 1);
+        gi.idx[1] = P.pstride + piece(P, 0, 0, 1);
+        cudaError_t e = c->gat.ensure(GATHER_MAX * sizeof(int64_t));
+        if (e == cudaSuccess) e = launch_gather(P.base, gi, (int64_t *)c->gat.ptr, c->stream);
+        int64_t h[2] = {0, 0};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, c->gat.ptr, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "halo counts");
+        v0 = h[0];
+        f0 = h[1];
+    }
+    if (v0 < 0 || v0 > c->nverts || f0 < 0 || f0 > c->nfaces) return fail(c, MESH_EDEVICE, "inconsistent halo counts");
+    c->nverts -= v0;
+    c->nfaces -= f0;
+    return MESH_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int mesh_count(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t nz, int vol_on_device,
                const mesh_params *p, int64_t *nverts, int64_t *nfaces) {
     if (!c || !nverts || !nfaces) return fail(c, MESH_EINVAL, "NULL argument");
@@ -798,6 +839,7 @@ int mesh_count(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int6
     c->nverts = c->h_misc[0];
     c->nfaces = c->h_misc[1];
     c->nactive = c->h_misc[2];
+    if (c->plan.xhalo && (rc = drop_halo_counts(c))) return rc;
     if (c->weld && (rc = run_weld(c))) return rc;
     *nverts = c->nverts;
     *nfaces = c->nfaces;
@@ -879,6 +921,7 @@ int mesh_extract_device(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t
     if (p->alg == MESH_ALG_MC_WELDED) return fail(c, MESH_EINVAL, "welded meshes are built by mesh_count / mesh_fill");
     if ((rc = prepare(c, vol, T, nx, ny, nz, 1, p))) return rc;
     Plan &P = c->plan;
+    if (P.xhalo) return fail(c, MESH_EINVAL, "an x window with a halo column is meshed by mesh_count / mesh_fill");
     P.verts = verts;
     P.faces = faces;
     P.verts_cap = verts ? verts_cap : 0;

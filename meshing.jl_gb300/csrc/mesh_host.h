@@ -83,6 +83,7 @@ struct mesh_ctx {
     // mesh_set_x_window: the volumes of the following calls are x nodes
     // win_x0 .. win_x0+nx-1 of an x axis of win_nx nodes (win_nx == 0: whole axis)
     int64_t win_x0 = 0, win_nx = 0;
+    int win_halo = 0;  // MT / NSN: the first cell column is the previous slab's last one
     std::string msg;
     // stage timing (diagnostics)
     int timing = 0;

@@ -115,6 +115,13 @@ struct Plan {
     int64_t nitems;
     int32_t nvols, nstiles;
     int32_t vol_outputs;  // 1: every volume writes to its own BatchVol::verts / faces
+    // x window (mesh_set_x_window): global x of the volume's sample 0, for the
+    // grid-boundary rules of MT / NSN; with xhalo, the volume's first cell column
+    // is the previous slab's last one -- counted (its vertices come first in the
+    // scan) but not emitted, and every emitted vertex, face and face index is
+    // shifted down by that column's totals (base of piece (seg 0, y 0, x 1))
+    int64_t xg0;
+    int32_t xhalo;
     // sub-range launches of the pipelined host path (zero: the whole volume):
     // classify z segments seg0 .. seg1 - 1; compact the x tiles tx0 .. tx0 + ntx - 1;
     // expand list entries e_lo .. e_hi - 1
