@@ -402,7 +402,9 @@ def run_ours(args, rank, world, dist):
     out_b = nv * 12 + nf * 24
     stage = {k: v[0] / args.steps for k, v in st.items()}  # each timed step runs every stage once
     # algorithmic bytes per launch (input 4 B per sample, mesh 12 B per vertex and
-    # 24 B per face): classify (k_classify) reads every sample; the scan reads 3
+    # 24 B per face): classify reads every sample (k_classify_tma_mc, staged by
+    # TMA, for volumes with 16-byte aligned rows; the load walk k_classify with
+    # MESHING_GB300_TMA=0); the scan reads 3
     # u32 counts and writes 3 int64 bases per piece; the direct emission
     # (k_direct_mc) writes the mesh (its second read of the samples of active
     # cells is not algorithmic and is not counted).  In the list form
@@ -411,7 +413,8 @@ def run_ours(args, rank, world, dist):
     # expansion (k_expand_mc) writes the mesh: only the expansion gets bytes.
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     kern = {
-        'classify': {'ms': stage['classify'], 'bytes': in_b, 'kernel': 'k_classify'},
+        'classify': {'ms': stage['classify'], 'bytes': in_b,
+                     'kernel': 'k_classify' if os.environ.get('MESHING_GB300_TMA') == '0' else 'k_classify_tma_mc'},
         'scan': {'ms': stage['scan'], 'bytes': float(pieces(n, n, n, sms) * 3 * (4 + 8)), 'kernel': 'k_scan'},
     }
     if stage.get('expand'):

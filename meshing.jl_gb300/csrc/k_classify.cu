@@ -606,6 +606,205 @@ __global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma(const Plan p,
     if (tid == 0 && s_fail) atomicOr(p.err, ERR_TMA_TIMEOUT);
 }
 
+// Marching Cubes walk over TMA-staged bricks (the default for volumes a tensor
+// map can describe).  The CTA's tile column -- 31 x-cells by WARPS * WY cell rows
+// of one z segment -- is streamed through the same TMA_STAGES-deep ring of
+// TMA_BZ-plane boxes as k_classify_tma, filled by one producer lane, so the
+// consumers never wait on a global load.  The consumer is the load walk's
+// guard-free form (classify_tile_mc_inner) reading shared memory: per stage
+// five row addresses, per plane one ballot per sample row and the plane's
+// AND / OR reduction (reused by the two steps that share the plane), per step
+// one packed-word lookup per cell row; an activity chunk (ZC = 2 stages)
+// closes at the first plane of every even stage.  Tiles at the volume's edge
+// take the same loop with per-lane and per-row guards.  Outputs as the load
+// walk: piece counts, activity bytes and the active-column masks (cmask).
+template <class T, bool INNER>
+__device__ __forceinline__ void tma_mc_consume(const Plan &p, const uint32_t *s_tab, const T *buf, uint64_t *full,
+                                               uint64_t *empty, int *s_fail, int lane, int w, int tx, int seg,
+                                               int xoff) {
+    constexpr int BX = TmaBox<T>::BX;
+    constexpr int PLANE = TMA_BY * BX;
+    constexpr int STAGE = (int)(tma_stage_bytes<T>() / sizeof(T));
+    const int ty = blockIdx.y * WARPS + w;
+    const int y0 = ty * WY;
+    const bool warp_on = ty < p.tiles_y;
+    const int xs = tx * TILE_X + lane;
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    const int nst = (zend - zbeg + 1 + TMA_BZ - 1) / TMA_BZ;  // stages of planes zbeg..zend
+    const bool cellx = lane < TILE_X && xs < p.cx;
+    bool rowok[WY + 1];
+    uint32_t rmask[WY];
+#pragma unroll
+    for (int r = 0; r <= WY; r++) rowok[r] = INNER || (xs < p.nx && y0 + r < p.ny);
+#pragma unroll
+    for (int r = 0; r < WY; r++) rmask[r] = (INNER ? lane < TILE_X : (cellx && y0 + r < p.cy)) ? 0xffffffffu : 0u;
+    const uint32_t xval = INNER ? FULL : __ballot_sync(FULL, xs < p.nx);
+    int off[WY + 1];  // the lane's sample of row r in a stage's first plane
+#pragma unroll
+    for (int r = 0; r <= WY; r++) off[r] = (w * WY + r) * BX + xoff + lane;
+    uint32_t cv[WY], cf[WY], ca[WY], pk[WY];
+#pragma unroll
+    for (int r = 0; r < WY; r++) cv[r] = cf[r] = ca[r] = pk[r] = 0;
+    uint32_t mlo[WY + 1], alo = 0, olo = 0;
+
+    auto masks = [&](const T *st, int k, uint32_t (&m)[WY + 1], uint32_t &a, uint32_t &o) {
+        a = xval;
+        o = 0;
+#pragma unroll
+        for (int r = 0; r <= WY; r++) {
+            m[r] = __ballot_sync(FULL, rowok[r] && below(st[k * PLANE + off[r]], p));
+            a &= m[r];
+            o |= m[r];
+        }
+    };
+    auto step = [&](const uint32_t (&mhi)[WY + 1], uint32_t ahi, uint32_t ohi) {
+        if ((alo & ahi) != xval && (olo | ohi) != 0u) {
+            uint32_t nb[WY + 1];
+#pragma unroll
+            for (int r = 0; r <= WY; r++) nb[r] = row_field(mlo[r], mhi[r], lane);
+#pragma unroll
+            for (int r = 0; r < WY; r++) pk[r] += s_tab[nb[r] | (nb[r + 1] << 4)] & rmask[r];
+        }
+#pragma unroll
+        for (int r = 0; r <= WY; r++) mlo[r] = mhi[r];
+        alo = ahi;
+        olo = ohi;
+    };
+    auto flush = [&](int ci) {  // close activity chunk ci of the segment
+        const int chunk = seg * p.chunks_per_seg + ci;
+        uint32_t mine = 0;  // lane r: the active columns of row y0 + r
+#pragma unroll
+        for (int r = 0; r < WY; r++) {
+            const uint32_t am = __ballot_sync(FULL, pk[r] != 0u);
+            if (lane == r) mine = am;
+            cv[r] += pk[r] & ((1u << PK_F) - 1u);
+            cf[r] += (pk[r] >> PK_F) & ((1u << (PK_A - PK_F)) - 1u);
+            ca[r] += pk[r] >> PK_A;
+            pk[r] = 0;
+        }
+        if (lane < WY && (INNER || y0 + lane < p.cy)) {
+            p.flags[((int64_t)chunk * p.tiles_x + tx) * p.cy + y0 + lane] = mine != 0u;
+            if (p.cmask) p.cmask[((int64_t)tx * p.cy + y0 + lane) * p.nchunks + chunk] = mine;
+        }
+    };
+    auto release = [&](int slot) {
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&empty[slot])) : "memory");
+    };
+
+    bool ok = true;
+    for (int s = 0; s < nst; s++) {
+        const int slot = s % TMA_STAGES;
+        ok = mbar_wait(&full[slot], (unsigned)(s / TMA_STAGES) & 1u);
+        ok = __all_sync(FULL, ok) && !*(volatile int *)s_fail;
+        if (!ok) {
+            if (lane == 0) atomicOr(s_fail, 1);
+            break;
+        }
+        const T *st = buf + slot * STAGE;
+        if (warp_on) {
+            const int p0 = zbeg + s * TMA_BZ;  // the stage's first plane
+            if (s == 0) {
+                masks(st, 0, mlo, alo, olo);
+#pragma unroll
+                for (int k = 1; k < TMA_BZ; k++) {
+                    if (p0 + k > zend) break;  // warp-uniform
+                    uint32_t mhi[WY + 1], ahi, ohi;
+                    masks(st, k, mhi, ahi, ohi);
+                    step(mhi, ahi, ohi);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < TMA_BZ; k++) {
+                    if (p0 + k > zend) break;  // warp-uniform
+                    uint32_t mhi[WY + 1], ahi, ohi;
+                    masks(st, k, mhi, ahi, ohi);
+                    step(mhi, ahi, ohi);
+                    // the step just taken ends an activity chunk (ZC == 2 * TMA_BZ)
+                    if (k == 0 && !(s & 1)) flush(s / 2 - 1);
+                }
+            }
+        }
+        release(slot);
+    }
+    if (!ok || !warp_on) return;
+    if ((zend - zbeg) % ZC) flush((zend - zbeg - 1) / ZC);  // the segment's last, shorter chunk
+    if (!cellx) return;
+    const int64_t np = p.pstride;
+#pragma unroll
+    for (int r = 0; r < WY; r++) {
+        if (INNER || y0 + r < p.cy) {
+            const int64_t i = piece(p, seg, y0 + r, xs);
+            p.cnt[i] = cv[r];
+            p.cnt[np + i] = cf[r];
+            p.cnt[2 * np + i] = ca[r];
+        }
+    }
+}
+static_assert(ZC == 2 * TMA_BZ, "an activity chunk is two TMA stages");
+
+template <class T>
+__global__ void __launch_bounds__(32 * (WARPS + 1)) k_classify_tma_mc(const Plan p, const __grid_constant__ CUtensorMap tmap) {
+    constexpr int AL = TmaBox<T>::ALIGN;
+    constexpr unsigned BYTES = TMA_BZ * TMA_BY * TmaBox<T>::BX * sizeof(T);  // one box
+    constexpr int STAGE = (int)(tma_stage_bytes<T>() / sizeof(T));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *buf = reinterpret_cast<T *>(smem_raw);  // [TMA_STAGES][STAGE]
+    __shared__ uint32_t s_tab[256];
+    __shared__ __align__(8) uint64_t full[TMA_STAGES], empty[TMA_STAGES];
+    __shared__ int s_fail;
+    load_tables_mc_packed(s_tab);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int tx = blockIdx.x, seg = blockIdx.z;
+    const int x0 = tx * TILE_X, xa = x0 & ~(AL - 1);
+    const int yc0 = blockIdx.y * WARPS * WY;
+    const int zbeg = seg * p.zs;
+    const int zend = min(zbeg + p.zs, p.cz);
+    const int nst = (zend - zbeg + 1 + TMA_BZ - 1) / TMA_BZ;
+    if (tid == 0) {
+        for (int k = 0; k < TMA_STAGES; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], WARPS);
+        }
+        s_fail = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (w == WARPS) {  // producer: one lane issues every stage's box
+        if (lane == 0) {
+            int issued = 0;
+            for (int s = 0; s < nst; s++) {
+                const int slot = s % TMA_STAGES;
+                if (s >= TMA_STAGES && !mbar_wait(&empty[slot], (unsigned)(s / TMA_STAGES - 1) & 1u)) {
+                    atomicOr(&s_fail, 1);
+                    break;
+                }
+                if (*(volatile int *)&s_fail) break;
+                fence_proxy_async();
+                mbar_expect_tx(&full[slot], BYTES);
+                tma_load_3d(buf + slot * STAGE, &tmap, xa, yc0, zbeg + s * TMA_BZ, &full[slot]);
+                issued = s + 1;
+            }
+            // on failure, let the copies in flight land before the CTA exits
+            if (*(volatile int *)&s_fail)
+                for (int s = max(0, issued - TMA_STAGES); s < issued; s++)
+                    mbar_wait(&full[s % TMA_STAGES], (unsigned)(s / TMA_STAGES) & 1u);
+        }
+        __syncwarp();
+    } else {
+        // inside the volume: all 32 lanes' samples and the WY + 1 sample rows exist
+        const int ty = blockIdx.y * WARPS + w;
+        const bool inner = x0 + 32 <= p.nx && ty * WY + WY <= p.cy;
+        if (inner)
+            tma_mc_consume<T, true>(p, s_tab, buf, full, empty, &s_fail, lane, w, tx, seg, x0 - xa);
+        else
+            tma_mc_consume<T, false>(p, s_tab, buf, full, empty, &s_fail, lane, w, tx, seg, x0 - xa);
+    }
+    __syncthreads();
+    if (tid == 0 && s_fail) atomicOr(p.err, ERR_TMA_TIMEOUT);
+}
+
 template <class T> cudaError_t launch_t(const Plan &p, cudaStream_t s) {
     const int ty = (p.cy + CWY - 1) / CWY;  // warp tiles of the load walk along y
     dim3 grid(p.tiles_x, (ty + WARPS - 1) / WARPS, p.nseg);
@@ -623,8 +822,8 @@ template <class T> cudaError_t launch_tma_t(const Plan &p, const CUtensorMap &ma
     cudaError_t e = cudaSuccess;
     switch (p.alg) {
     case MESH_ALG_MC:
-        e = cudaFuncSetAttribute(k_classify_tma<T, MESH_ALG_MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e == cudaSuccess) k_classify_tma<T, MESH_ALG_MC><<<grid, 32 * (WARPS + 1), sm, s>>>(p, map);
+        e = cudaFuncSetAttribute(k_classify_tma_mc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess) k_classify_tma_mc<T><<<grid, 32 * (WARPS + 1), sm, s>>>(p, map);
         break;
     case MESH_ALG_MT:
         e = cudaFuncSetAttribute(k_classify_tma<T, MESH_ALG_MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

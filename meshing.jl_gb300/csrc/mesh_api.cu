@@ -265,7 +265,7 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
     // least PIPE_MAX segments, so that all but the last group's classification
     // runs under the upload (a mapped host volume read in place is not uploaded)
     const size_t vbytes0 = (size_t)nx * ny * nz * dtype_size(T);
-    if (!vol_on_device && !c->zerocopy && c->pipe_bytes > 0 && (int64_t)vbytes0 >= c->pipe_bytes && !c->want_tma &&
+    if (!vol_on_device && !c->zerocopy && c->pipe_bytes > 0 && (int64_t)vbytes0 >= c->pipe_bytes && c->tma_env != 1 &&
         !c->one_walk)
         nseg = std::min(maxseg, std::max(nseg, PIPE_MAX));
     int zs = (P.cz + nseg - 1) / nseg;
@@ -293,7 +293,7 @@ int prepare(mesh_ctx *c, const void *vol, int T, int64_t nx, int64_t ny, int64_t
         cudaGetLastError();
         if ((e = c->vol.ensure(vbytes)) != cudaSuccess) return cuda_fail(c, e, "volume buffer");
         P.vol = c->vol.ptr;
-        if (c->pipe_bytes > 0 && (int64_t)vbytes >= c->pipe_bytes && P.nseg >= 2 && !c->want_tma && !c->one_walk) {
+        if (c->pipe_bytes > 0 && (int64_t)vbytes >= c->pipe_bytes && P.nseg >= 2 && c->tma_env != 1 && !c->one_walk) {
             int rc = ensure_pipe(c);
             if (rc) return rc;
             c->ngroups = std::min(PIPE_MAX, P.nseg);  // the count uploads and classifies
@@ -390,7 +390,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // boundaries and the volume must be at least one box large.
 bool make_tensor_map(mesh_ctx *c) {
     const Plan &P = c->plan;
-    if (!c->want_tma) return false;
+    if (!(c->tma_env == 1 || (c->tma_env < 0 && P.alg == MESH_ALG_MC))) return false;
     int bx;
     size_t es;
     CUtensorMapDataType dt;
@@ -421,9 +421,9 @@ bool one_walk(const mesh_ctx *c) {
 
 // Marching Cubes emitted straight from the volume (the default): the classify
 // walk leaves per-chunk active-column masks and no list of active cells is
-// built.  The opt-in TMA walk writes no masks and takes the list form.
+// built (both classify walks write the masks).
 bool direct_mc(const mesh_ctx *c) {
-    return c->plan.alg == MESH_ALG_MC && !c->list_emit && !c->want_tma && !one_walk(c);
+    return c->plan.alg == MESH_ALG_MC && !c->list_emit && !one_walk(c);
 }
 
 int run_count(mesh_ctx *c) {
@@ -431,7 +431,8 @@ int run_count(mesh_ctx *c) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(c->misc.ptr, 0, MISC_SLOTS * sizeof(int64_t), c->stream)) != cudaSuccess)
         return cuda_fail(c, e, "memset");
-    c->use_tma = !one_walk(c) && make_tensor_map(c);
+    // the pipelined upload classifies each group with the load walk as it arrives
+    c->use_tma = !one_walk(c) && c->ngroups == 1 && make_tensor_map(c);
     mark(c, 0);
     int nlaunch = 1;
     if (one_walk(c)) {
@@ -668,7 +669,7 @@ int mesh_ctx_create(int device, mesh_ctx **out) {
     const char *ff = getenv("MESHING_GB300_FORCE_FP64");
     c->force_fp64 = ff && ff[0] == '1';
     const char *wt = getenv("MESHING_GB300_TMA");
-    c->want_tma = wt && wt[0] == '1';
+    c->tma_env = (wt && wt[0] == '1') ? 1 : (wt && wt[0] == '0') ? 0 : -1;
     const char *ow = getenv("MESHING_GB300_ONE_WALK");
     c->one_walk = ow && ow[0] == '1';
     const char *le = getenv("MESHING_GB300_LIST_EMIT");

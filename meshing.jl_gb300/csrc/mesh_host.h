@@ -88,9 +88,11 @@ struct mesh_ctx {
     // stage timing (diagnostics)
     int timing = 0;
     int force_fp64 = 0;  // MESHING_GB300_FORCE_FP64=1: evaluate every Float64 position in FP64
-    // MESHING_GB300_TMA=1: classify from TMA-staged bricks.  Off by default: on
-    // GB300 the plain global-load walk is faster (1.24 vs 1.29 ms at 1024^3 f32).
-    int want_tma = 0;
+    // Classification from TMA-staged bricks: by default for Marching Cubes volumes a
+    // tensor map can describe (Float32 / UInt16 / Float64, 16-byte row strides) and
+    // not uploaded in pipelined groups; MESHING_GB300_TMA=0 (-1 unset) keeps the
+    // global-load walk, MESHING_GB300_TMA=1 also streams MT / NSN volumes.
+    int tma_env = -1;
     // MESHING_GB300_ONE_WALK=1: Marching Cubes in one walk that also lists the
     // active cells (k_walk_mc.cu).  Off by default: on GB300 the walk is issue
     // bound, so dropping the second read of the volume saves little, and

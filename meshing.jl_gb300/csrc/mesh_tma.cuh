@@ -15,9 +15,10 @@ constexpr unsigned ERR_TMA_TIMEOUT = 8u;
 constexpr int TMA_SPIN_LIMIT = 1 << 20;  // polls of ~1 us each at most
 
 // Box of one volume stage: BX samples in x (a multiple of 16 bytes, starting on
-// a 16-byte boundary), BY sample rows, BZ planes.
+// a 16-byte boundary at or below the tile's first sample: the 32 samples of a
+// warp tile plus the rounding, at most ALIGN - 1), BY sample rows, BZ planes.
 template <class T> struct TmaBox;
-template <> struct TmaBox<float> { static constexpr int BX = 40, ALIGN = 4; };
+template <> struct TmaBox<float> { static constexpr int BX = 36, ALIGN = 4; };
 template <> struct TmaBox<uint16_t> { static constexpr int BX = 40, ALIGN = 8; };
 template <> struct TmaBox<double> { static constexpr int BX = 34, ALIGN = 2; };
 constexpr int TMA_BY = 8 * WY + 1;  // the CTA's 32 cell rows + 1

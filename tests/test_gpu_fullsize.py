@@ -124,20 +124,53 @@ def test_ct_u16_512_whole_mesh_bit_exact(pkg, oracle, cuda):
 
 @pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
 def test_tma_walk_matches_global_load_walk(pkg, cuda, alg, monkeypatch):
-    # with MESHING_GB300_TMA=1 volumes with 16-byte aligned rows are classified
-    # from TMA-staged bricks; the default plain global-load walk must give the
-    # same mesh
+    # volumes with 16-byte aligned rows are classified from TMA-staged bricks
+    # (by default for MarchingCubes; MESHING_GB300_TMA=1 for all, =0 for none);
+    # the plain global-load walk must give the same mesh
     torch = cuda
     import meshing_gb300.fields as fields
     t = fields.gyroid(192, dtype=torch.float32)
     m = {'mc': pkg.MarchingCubes, 'nsn': pkg.NaiveSurfaceNets}.get(alg, pkg.MarchingTetrahedra)(iso=np.float32(0))
-    v1, f1 = run_device(torch, pkg, t, m, ((0, 1),) * 3)
-    monkeypatch.setenv('MESHING_GB300_TMA', '1')
-    ctx = pkg.Context(0)
-    v2, f2 = run_device(torch, pkg, t, m, ((0, 1),) * 3, ctx=ctx)
-    ctx.close()
-    assert f1.shape[0] > 0
-    assert torch.equal(f1, f2) and torch.equal(v1, v2)
+    got = {}
+    for env in ('0', '1'):
+        monkeypatch.setenv('MESHING_GB300_TMA', env)
+        ctx = pkg.Context(0)
+        got[env] = run_device(torch, pkg, t, m, ((0, 1),) * 3, ctx=ctx)
+        ctx.close()
+    assert got['0'][1].shape[0] > 0
+    assert torch.equal(got['0'][1], got['1'][1]) and torch.equal(got['0'][0], got['1'][0])
+
+
+@pytest.mark.parametrize('shape,dt,iso', [
+    ((36, 33, 4), 'f32', np.float32(0.02)),       # one box, one stage
+    ((100, 70, 45), 'f32', np.float32(-0.1)),     # ragged tiles, a short last stage
+    ((128, 97, 203), 'f32', np.float32(0.3)),     # several segments, partial rows of CTAs
+    ((64, 41, 61), 'f64', 0.0),
+    ((96, 50, 77), 'u16', 500),
+])
+def test_tma_marching_cubes_walk_on_ragged_volumes(pkg, oracle, cuda, shape, dt, iso, monkeypatch):
+    # the Marching Cubes TMA walk (default) against the load walk and the oracle,
+    # bit for bit, on shapes that exercise edge tiles, short stages and chunks
+    torch = cuda
+    rng = np.random.default_rng(sum(shape))
+    g = [np.linspace(-1, 1, n) for n in shape]
+    X, Y, Z = np.meshgrid(*g, indexing='ij')
+    f = np.sin(5 * X) * np.cos(4 * Y + 0.3) + np.sin(3 * Z) * np.cos(5 * X) + 0.05 * rng.standard_normal(shape)
+    A = {'f32': f.astype(np.float32), 'f64': f, 'u16': np.round((f + 2) * 250).astype(np.uint16)}[dt]
+    A = np.asfortranarray(A)
+    vol = torch.from_numpy(np.ascontiguousarray(A.transpose(2, 1, 0))).cuda().permute(2, 1, 0)
+    m = pkg.MarchingCubes(iso=iso)
+    got = {}
+    for env in ('1', '0'):
+        monkeypatch.setenv('MESHING_GB300_TMA', env)
+        ctx = pkg.Context(0)
+        got[env] = run_device(torch, pkg, vol, m, ((-1, 1),) * 3, ctx=ctx)
+        ctx.close()
+    wv, wf = oracle.isosurface(A, 'mc', iso, 1e-3, ((-1, 1),) * 3)
+    assert len(wf) > 0
+    for env in ('1', '0'):
+        assert np.array_equal(got[env][1].cpu().numpy(), wf), env
+        assert np.array_equal(got[env][0].cpu().numpy().view(np.uint8), wv.view(np.uint8)), env
 
 
 def test_u8_1700_past_2_32_samples_whole_mesh_bit_exact(pkg, oracle, cuda):
