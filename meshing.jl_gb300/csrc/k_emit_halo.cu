@@ -41,20 +41,32 @@ constexpr int R = WY + 1;  // cell rows per tile including the -y neighbour row
 struct MtTables {
     uint8_t faces[256][3 * MT_MAX_FACES];
     uint8_t order[256][MT_MAX_TOUCH];
-    uint32_t before[256][19];
     uint32_t touched[256];
     uint8_t nfaces[256];
     uint8_t za[19];          // axes on which both corners of the edge are 0
     uint8_t shifted[19][8];  // the same lattice edge seen from the cell shifted by -s
+    uint8_t kth0[256][MT_MAX_TOUCH];  // interior cells: the k-th owned edge in first-use order
 };
 
 // One warp's state of a z step.
 template <class T> struct HaloWarp {
     T samp[2][R + 1][32];        // samples of plane z (samp[cur ^ 1]) and z+1 (samp[cur])
-    uint32_t cas[2][R][32];      // cases of the cells of planes z-1 (cur ^ 1) and z (cur)
+    uint8_t cas[2][R][32];       // cases of the cells of planes z-1 (cur ^ 1) and z (cur)
     long long base[2][R][32];    // their first vertex
     long long fbase[R][32];      // first face of the cells of plane z
     uint16_t pv[R * 32], pf[R * 32];  // inclusive prefix of vertex / face tasks over (row, lane)
+};
+
+// NSN: one round of up to 32 vertex tasks as (cell, crossed edge) pairs.
+struct NsnPairs {
+    int end[32];         // inclusive prefix of the round's lanes' pair counts
+    uint32_t cell[32];   // crossed-edge mask | lane << 12 | row << 17 of the lane's cell
+    double pt[32][3];    // crossing points of a sub-round of 32 pairs
+    // vertices whose sums are complete, waiting for their mean: divided 32 at
+    // a time, so that the Float64 divisions run with full warps across steps
+    double qs[32][3];
+    long long qv[32];
+    uint8_t qn[32];
 };
 
 // First entry of the inclusive prefix a[0..n) above t (a[n-1] > t).
@@ -103,17 +115,22 @@ __device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int
 }
 
 template <class T, class Q, class A, class P, int ALG>
-__global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
+__global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh) {
     extern __shared__ __align__(16) unsigned char smem[];
     HaloWarp<T> *ws_all = reinterpret_cast<HaloWarp<T> *>(smem);
-    MtTables *tb = reinterpret_cast<MtTables *>(smem + sizeof(HaloWarp<T>) * WARPS);
+    MtTables *tb = reinterpret_cast<MtTables *>(smem + sizeof(HaloWarp<T>) * WARPS);  // MT
+    NsnPairs *prs = reinterpret_cast<NsnPairs *>(smem + sizeof(HaloWarp<T>) * WARPS);  // NSN
     if (ALG == MESH_ALG_MT) {
         for (int i = threadIdx.x; i < 256; i += blockDim.x) {
             for (int k = 0; k < 3 * MT_MAX_FACES; k++) tb->faces[i][k] = MT_CASE_FACES[i][k];
             for (int k = 0; k < MT_MAX_TOUCH; k++) tb->order[i][k] = MT_TOUCH_ORDER[i][k];
-            for (int k = 0; k < 19; k++) tb->before[i][k] = MT_BEFORE[i][k];
             tb->touched[i] = MT_TOUCHED[i];
             tb->nfaces[i] = MT_CASE_NFACES[i];
+            const int nt = __popc(MT_TOUCHED[i]);
+            for (int k = 0, seen = 0; k < nt; k++) {
+                const int ee = MT_TOUCH_ORDER[i][k];
+                if ((p.own[0] >> ee) & 1u) tb->kth0[i][seen++] = (uint8_t)ee;
+            }
         }
         if (threadIdx.x < 19) {
             const int e = threadIdx.x;
@@ -227,6 +244,19 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
         }
     };
 
+    // NSN: queued vertices (a warp-uniform count) and their means, lane i taking entry i
+    int qcount = 0;
+    auto nsn_means = [&](int m) {
+        if (ALG != MESH_ALG_NSN) return;
+        NsnPairs &pr = prs[wid];
+        if (lane < m) {
+            const P n = (P)pr.qn[lane];
+            store_vert(p, pr.qv[lane], Ar<P>::div((P)pr.qs[lane][0], n), Ar<P>::div((P)pr.qs[lane][1], n),
+                       Ar<P>::div((P)pr.qs[lane][2], n));
+        }
+        __syncwarp();
+    };
+
     uint32_t mlo[R + 1];
     bool have_lo = false;
     int cur = 0;  // buffer of plane z+1 samples / plane z cells; cur ^ 1 holds plane z / plane z-1
@@ -262,7 +292,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                     unsigned cs;
                     int nv, nf;
                     classify(pm, mlo, r, zc0 - 1, cs, nv, nf);
-                    ws.cas[cur ^ 1][r][lane] = cs;
+                    ws.cas[cur ^ 1][r][lane] = (uint8_t)cs;
                     ws.base[cur ^ 1][r][lane] = bv[r] - nv;
                 }
             } else {
@@ -281,7 +311,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 classify(mlo, mhi, r, zc, cs[r], nvs[r], nfs[r]);
-                ws.cas[cur][r][lane] = cs[r];
+                ws.cas[cur][r][lane] = (uint8_t)cs[r];
                 ws.base[cur][r][lane] = bv[r];
                 ws.fbase[r][lane] = bf[r];
                 any |= r >= 1 && realx && cs[r] != 0u;
@@ -316,28 +346,32 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                 __syncwarp();
                 const int lo_b = cur ^ 1, hi_b = cur;
                 // vertices
-                for (int t = lane; t < accv; t += 32) {
-                    const int sc = task_cell(ws.pv, R * 32, t);
-                    const int r = sc >> 5, l = sc & 31;
-                    const int k = t - (sc ? (int)ws.pv[sc - 1] : 0);
-                    const unsigned c = ws.cas[cur][r][l];
-                    const int xc = x0 + l, yc = y0 - 1 + r;
-                    const int64_t vb = ws.base[cur][r][l] - V0;  // this volume's first emitted vertex is 0
-                    P q[3];
-                    if (ALG == MESH_ALG_MT) {
+                if (ALG == MESH_ALG_MT) {
+                    for (int t = lane; t < accv; t += 32) {
+                        const int sc = task_cell(ws.pv, R * 32, t);
+                        const int r = sc >> 5, l = sc & 31;
+                        const int k = t - (sc ? (int)ws.pv[sc - 1] : 0);
+                        const unsigned c = ws.cas[cur][r][l];
+                        const int xc = x0 + l, yc = y0 - 1 + r;
+                        const int64_t vb = ws.base[cur][r][l] - V0;  // this volume's first emitted vertex is 0
+                        P q[3];
                         const int bnd = (xc + p.xg0 == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
                         const uint32_t own = p.own[bnd];
                         // the k-th owned edge in the cell's first-use order
-                        const int nt = __popc(tb->touched[c]);
-                        int e = 0, seen = 0;
-                        for (int i = 0; i < nt; i++) {
-                            const int ee = tb->order[c][i];
-                            if (!((own >> ee) & 1u)) continue;
-                            if (seen == k) {
-                                e = ee;
-                                break;
+                        int e = 0;
+                        if (bnd == 0) {
+                            e = tb->kth0[c][k];
+                        } else {
+                            const int nt = __popc(tb->touched[c]);
+                            for (int i = 0, seen = 0; i < nt; i++) {
+                                const int ee = tb->order[c][i];
+                                if (!((own >> ee) & 1u)) continue;
+                                if (seen == k) {
+                                    e = ee;
+                                    break;
+                                }
+                                seen++;
                             }
-                            seen++;
                         }
                         // MT corner order: (x,y,z) (x,y+1,z) (x+1,y+1,z) (x+1,y,z), then z+1
                         const int i1 = MT_EDGE_CORNERS[e][0], i2 = MT_EDGE_CORNERS[e][1];
@@ -347,32 +381,98 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                         };
                         mt_point<T, Q, A, P>(p, e, xc, yc, zc, corner(i1), corner(i2), q);
                         store_vert(p, vb + k, q[0], q[1], q[2]);
-                    } else {
-                        // NSN: the mean of the crossing points on the crossed MC edges
-                        const T cv[8] = {ws.samp[lo_b][r][l],     ws.samp[lo_b][r][l + 1],
-                                         ws.samp[lo_b][r + 1][l + 1], ws.samp[lo_b][r + 1][l],
-                                         ws.samp[hi_b][r][l],     ws.samp[hi_b][r][l + 1],
-                                         ws.samp[hi_b][r + 1][l + 1], ws.samp[hi_b][r + 1][l]};
-                        // crossed MC edges as a bit mask (edges 0-7 join corners e, e+1 of
-                        // their face ring, 8-11 join e-8 and e-4), summed in edge order
+                    }
+                } else {
+                    // NSN: the mean of the crossing points on the cell's crossed MC edges,
+                    // summed in edge order.  A round of 32 cells is expanded into its
+                    // (cell, crossed edge) pairs, so that the Float64 quotient of every
+                    // crossing runs with full warps; each lane then adds its cell's
+                    // points in edge order from shared memory.
+                    NsnPairs &pr = prs[wid];
+                    for (int t0 = 0; t0 < accv; t0 += 32) {
+                        const int t = t0 + lane;
+                        int r = 0, l = 0, n = 0;
                         unsigned crossed = 0;
+                        if (t < accv) {
+                            const int sc = task_cell(ws.pv, R * 32, t);
+                            r = sc >> 5;
+                            l = sc & 31;
+                            const unsigned c = ws.cas[cur][r][l];
+                            // crossed MC edges as a bit mask (edges 0-7 join corners e, e+1 of
+                            // their face ring, 8-11 join e-8 and e-4)
 #pragma unroll
-                        for (int e = 0; e < 12; e++) {
-                            const int ea = e < 8 ? (e & 3) + (e & 4) : e - 8;
-                            const int eb = e < 8 ? ((e + 1) & 3) + (e & 4) : e - 4;
-                            crossed |= (((c >> ea) ^ (c >> eb)) & 1u) << e;
+                            for (int e = 0; e < 12; e++) {
+                                const int ea = e < 8 ? (e & 3) + (e & 4) : e - 8;
+                                const int eb = e < 8 ? ((e + 1) & 3) + (e & 4) : e - 4;
+                                crossed |= (((c >> ea) ^ (c >> eb)) & 1u) << e;
+                            }
+                            n = __popc(crossed);
                         }
+                        int inc = n;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int a = __shfl_up_sync(FULL, inc, o);
+                            if (lane >= o) inc += a;
+                        }
+                        const int S = __shfl_sync(FULL, inc, 31), beg = inc - n;
+                        pr.end[lane] = inc;
+                        pr.cell[lane] = crossed | ((unsigned)l << 12) | ((unsigned)r << 17);
+                        __syncwarp();
                         P sum[3] = {P(0), P(0), P(0)};
-                        const int n = __popc(crossed);
-                        while (crossed) {
-                            const int e = __ffs(crossed) - 1;
-                            crossed &= crossed - 1;
-                            mc_point<T, Q, P>(p, e, xc, yc, zc, cv, q);
+                        for (int j0 = 0; j0 < S; j0 += 32) {
+                            const int j = j0 + lane;
+                            if (j < S) {
+                                // the pair's lane: the first whose inclusive end exceeds j
+                                int lo = 0, hi = 31;
+                                while (lo < hi) {
+                                    const int mid = (lo + hi) >> 1;
+                                    if (pr.end[mid] > j) hi = mid;
+                                    else lo = mid + 1;
+                                }
+                                const unsigned cw = pr.cell[lo];
+                                const int k = j - (lo ? pr.end[lo - 1] : 0);
+                                const int e = (int)__fns(cw & 0xfffu, 0, k + 1);
+                                const int r2 = (int)(cw >> 17), l2 = (int)((cw >> 12) & 31u);
+                                const McEdge g = mc_edge(e);
+                                const int ca = mc_corner_off(g.a), cb = mc_corner_off(g.b);
+                                const T va = ws.samp[(ca & 4) ? hi_b : lo_b][r2 + ((ca >> 1) & 1)][l2 + (ca & 1)];
+                                const T vbv = ws.samp[(cb & 4) ? hi_b : lo_b][r2 + ((cb >> 1) & 1)][l2 + (cb & 1)];
+                                P q[3];
+                                mc_edge_point<T, Q, P>(p, g, x0 + l2, y0 - 1 + r2, zc, va, vbv, q);
+                                pr.pt[lane][0] = (double)q[0];
+                                pr.pt[lane][1] = (double)q[1];
+                                pr.pt[lane][2] = (double)q[2];
+                            }
+                            __syncwarp();
+                            const int qa = max(beg, j0), qb = min(inc, j0 + 32);
+                            for (int qq = qa; qq < qb; qq++) {
 #pragma unroll
-                            for (int kk = 0; kk < 3; kk++) sum[kk] = Ar<P>::add(sum[kk], q[kk]);
+                                for (int kk = 0; kk < 3; kk++) sum[kk] = Ar<P>::add(sum[kk], (P)pr.pt[qq - j0][kk]);
+                            }
+                            __syncwarp();
                         }
-                        store_vert(p, vb, Ar<P>::div(sum[0], (P)n), Ar<P>::div(sum[1], (P)n),
-                                   Ar<P>::div(sum[2], (P)n));
+                        // lanes 0 .. m - 1 hold finished sums: queue them, dividing 32
+                        // at a time (the lanes past the queue's room wait for the flush)
+                        const int m = min(32, accv - t0);
+                        const int64_t vq = t < accv ? ws.base[cur][r][l] - V0 : 0;  // this volume's first vertex is 0
+                        auto push = [&](bool mine, int slot) {
+                            if (mine) {
+                                pr.qs[slot][0] = (double)sum[0];
+                                pr.qs[slot][1] = (double)sum[1];
+                                pr.qs[slot][2] = (double)sum[2];
+                                pr.qv[slot] = vq;
+                                pr.qn[slot] = (uint8_t)n;
+                            }
+                        };
+                        push(lane < m && qcount + lane < 32, qcount + lane);
+                        if (qcount + m >= 32) {
+                            __syncwarp();
+                            nsn_means(32);
+                            push(lane < m && qcount + lane >= 32, qcount + lane - 32);
+                            qcount -= 32;
+                        }
+                        qcount += m;
+                        __syncwarp();
                     }
                 }
                 // faces
@@ -393,7 +493,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                             const int e = tb->faces[c][3 * f + j];
                             const int sh = tb->za[e] & ~bnd;
                             if (sh == 0) {
-                                id[j] = vb + __popc(tb->before[c][e] & own) + 1;
+                                id[j] = vb + __popc(__ldg(&MT_BEFORE[c][e]) & own) + 1;
                             } else {
                                 // owned by the neighbour one step back along the axes of sh
                                 const int e2 = tb->shifted[e][sh];
@@ -403,7 +503,7 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
                                 const int64_t base2 = ws.base[b2][r2][l2] - V0;
                                 const int bnd2 = ((xc - (sh & 1) + p.xg0) == 0) | (((yc - ((sh >> 1) & 1)) == 0) << 1) |
                                                  (((zc - ((sh >> 2) & 1)) == 0) << 2);
-                                id[j] = base2 + __popc(tb->before[c2][e2] & p.own[bnd2]) + 1;
+                                id[j] = base2 + __popc(__ldg(&MT_BEFORE[c2][e2]) & p.own[bnd2]) + 1;
                             }
                         }
                         o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
@@ -453,12 +553,13 @@ __global__ void __launch_bounds__(256) k_emit_halo(const Plan p, int tiles_xh) {
             cur ^= 1;
         }
     }
+    if (qcount > 0) nsn_means(qcount);
 }
 
 template <class T, class Q, class A, class P, int ALG> cudaError_t go(const Plan &p, cudaStream_t s) {
     const int txh = (p.cx + TILE_XH - 1) / TILE_XH;
     dim3 grid(txh, (p.tiles_y + WARPS - 1) / WARPS, p.nseg);
-    const size_t sm = sizeof(HaloWarp<T>) * WARPS + (ALG == MESH_ALG_MT ? sizeof(MtTables) : 0);
+    const size_t sm = sizeof(HaloWarp<T>) * WARPS + (ALG == MESH_ALG_MT ? sizeof(MtTables) : WARPS * sizeof(NsnPairs));
     cudaError_t e = cudaFuncSetAttribute(k_emit_halo<T, Q, A, P, ALG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sm);
     if (e != cudaSuccess) return e;
