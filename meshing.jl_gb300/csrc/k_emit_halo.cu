@@ -18,7 +18,7 @@
 //
 // Tiling: 30 x-cells (lanes 1..30) plus the -x neighbour (lane 0) by WY
 // y-cells plus the -y neighbour row, one z segment; lane 31 only supplies
-// samples.  Per z step the warp classifies its cells lane by lane, then
+// samples.  Warps are persistent and take their tiles from a work counter.  Per z step the warp classifies its cells lane by lane, then
 // stages the step in its shared memory -- the sample values of both planes,
 // the cases and vertex bases of the current and previous plane, each cell's
 // first face -- with the inclusive prefix of the cells' vertex and face
@@ -30,6 +30,9 @@
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
 #include "mesh_point.cuh"
+
+#include <algorithm>
+#include <mutex>
 
 namespace mesh {
 
@@ -162,11 +165,10 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
 
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
-    const int ty = blockIdx.y * WARPS + wid;
-    if (ty >= p.tiles_y) return;
     HaloWarp<T> &ws = ws_all[wid];
-    const int tx = blockIdx.x;
-    const int seg = blockIdx.z;
+
+    // one warp tile: x tile tx, y tile ty, z segment seg
+    auto halo_tile = [&](int tx, int ty, int seg) {
     const int x0 = tx * TILE_XH - 1;         // x of lane 0 (the -x neighbour cell)
     const int xs = x0 + lane;                // sample / cell x of this lane
     const int y0 = ty * WY;                  // first real cell row; row 0 of the tile is y0-1
@@ -554,16 +556,56 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
         }
     }
     if (qcount > 0) nsn_means(qcount);
+    };
+
+    // persistent warps: tiles are taken from a work counter, x tile fastest
+    const int nitems = tiles_xh * p.tiles_y * p.nseg;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(p.work, 1u);
+        item = __shfl_sync(FULL, item, 0);
+        if (item >= nitems) break;
+        __syncwarp();  // the previous tile is done with the warp's shared state
+        halo_tile(item % tiles_xh, (item / tiles_xh) % p.tiles_y, item / (tiles_xh * p.tiles_y));
+    }
+}
+
+template <class T, int ALG> constexpr size_t halo_smem() {
+    return sizeof(HaloWarp<T>) * WARPS + (ALG == MESH_ALG_MT ? sizeof(MtTables) : WARPS * sizeof(NsnPairs));
+}
+
+// Resident CTAs of k_emit_halo<T, Q, A, P, ALG> on the current device, with its
+// dynamic shared memory allowed (one-time per device and instantiation).
+template <class T, class Q, class A, class P, int ALG> int halo_grid() {
+    static std::mutex mu;
+    static int grid[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!grid[dev]) {
+        const void *fn = (const void *)k_emit_halo<T, Q, A, P, ALG>;
+        const int smem = (int)halo_smem<T, ALG>();
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * WARPS, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        cudaGetLastError();
+        grid[dev] = per_sm * sms;
+    }
+    return grid[dev];
 }
 
 template <class T, class Q, class A, class P, int ALG> cudaError_t go(const Plan &p, cudaStream_t s) {
     const int txh = (p.cx + TILE_XH - 1) / TILE_XH;
-    dim3 grid(txh, (p.tiles_y + WARPS - 1) / WARPS, p.nseg);
-    const size_t sm = sizeof(HaloWarp<T>) * WARPS + (ALG == MESH_ALG_MT ? sizeof(MtTables) : WARPS * sizeof(NsnPairs));
-    cudaError_t e = cudaFuncSetAttribute(k_emit_halo<T, Q, A, P, ALG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm);
-    if (e != cudaSuccess) return e;
-    k_emit_halo<T, Q, A, P, ALG><<<grid, 32 * WARPS, sm, s>>>(p, txh);
+    const int64_t nitems = (int64_t)txh * p.tiles_y * p.nseg;
+    const int grid = halo_grid<T, Q, A, P, ALG>();
+    if (grid < 1) return cudaErrorInvalidDevice;
+    cudaError_t e = cudaMemsetAsync(p.work, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess || nitems < 1) return e;
+    const int ctas = (int)std::min<int64_t>(grid, (nitems + WARPS - 1) / WARPS);
+    k_emit_halo<T, Q, A, P, ALG><<<ctas, 32 * WARPS, halo_smem<T, ALG>(), s>>>(p, txh);
     return cudaGetLastError();
 }
 
