@@ -40,6 +40,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int R = WY + 1;  // cell rows per tile including the -y neighbour row
+constexpr int NSN_VC = 10; // NSN: cells per vertex round (three lanes per cell add up its points)
 
 struct MtTables {
     uint8_t faces[256][3 * MT_MAX_FACES];
@@ -57,7 +58,7 @@ template <class T> struct HaloWarp {
     uint8_t cas[2][R][32];       // cases of the cells of planes z-1 (cur ^ 1) and z (cur)
     long long base[2][R][32];    // their first vertex
     long long fbase[R][32];      // first face of the cells of plane z
-    uint16_t pv[R * 32], pf[R * 32];  // inclusive prefix of vertex / face tasks over (row, lane)
+    uint16_t pv[R * 32], pf[R * 32];  // inclusive prefix of vertex / face tasks over (lane, row)
 };
 
 // NSN: one round of up to 32 vertex tasks as (cell, crossed edge) pairs.
@@ -93,6 +94,24 @@ __device__ __forceinline__ unsigned mt_case(unsigned a, unsigned b, unsigned c, 
 }
 
 
+template <class A> __device__ __forceinline__ bool is_zero(A v);
+template <> __device__ __forceinline__ bool is_zero<float>(float v) { return (__float_as_uint(v) << 1) == 0u; }
+template <> __device__ __forceinline__ bool is_zero<double>(double v) {
+    return ((unsigned long long)__double_as_longlong(v) << 1) == 0ull;
+}
+
+// c1*b + c2*a in A, with the corner coordinates c1, c2 in {0, 1} and a, b not
+// NaN: the products are b or a (times 1) and zeros carrying the sign of b or a
+// (times 0), so the sum is ab = b + a (both 1), or one term plus a zero -- the
+// other term, or the IEEE sum of two zeros -- with no arithmetic.
+template <class A> __device__ __forceinline__ A corner_mix(int c1, int c2, A b, A a, A ab) {
+    if (c1 && c2) return ab;
+    const A t1 = c1 ? b : copysign(A(0), b), t2 = c2 ? a : copysign(A(0), a);
+    if (!is_zero<A>(t1)) return t1;  // t2 is a zero
+    if (!is_zero<A>(t2)) return t2;
+    return (signbit(t1) && signbit(t2)) ? -A(0) : A(0);
+}
+
 // vertPos (src/marching_tetrahedra.jl:42-55) for voxel edge e of cell (x,y,z)
 // with the values sv, tv at the edge's corners (MT corner order).
 template <class T, class Q, class A, class P>
@@ -103,6 +122,8 @@ __device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int
     const A hi = sizeof(A) == 4 ? (A)p.hi_f : (A)p.hi_d;
     const A a = jl_min<A>(jl_max<A>((A)q, eps), hi);
     const A b = Ar<A>::sub(A(1), a);
+    const bool nan = isnan(a);  // then b and every weight are NaN
+    const A ab = Ar<A>::add(b, a);
     const int idx[3] = {x, y, z};
     const double *tp[3] = {p.xp, p.yp, p.zp};
     const double *td[3] = {p.dx, p.dy, p.dz};
@@ -110,7 +131,7 @@ __device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int
     const float *tdf[3] = {p.dxf, p.dyf, p.dzf};
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const A w = Ar<A>::add(Ar<A>::mul((A)MT_CORNER_POS[i1][k], b), Ar<A>::mul((A)MT_CORNER_POS[i2][k], a));
+        const A w = nan ? a : corner_mix<A>(MT_CORNER_POS[i1][k], MT_CORNER_POS[i2][k], b, a, ab);
         const P base = tab<P>(tp[k], tpf[k], idx[k]);
         const P d = tab<P>(td[k], tdf[k], idx[k]);
         r[k] = Ar<P>::add(base, Ar<P>::mul((P)w, d));
@@ -319,31 +340,39 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                 any |= r >= 1 && realx && cs[r] != 0u;
             }
             if (__any_sync(FULL, any)) {
-                // tasks of the real cells (rows 1.., lanes 1..30): inclusive prefix over (row, lane)
-                int accv = 0, accf = 0;
+                // tasks of the real cells (rows 1.., lanes 1..30), in (lane, row) order
+                // (each task writes to its cell's own outputs, so any order will do):
+                // one scan of the lane's packed vertex | face << 16 totals, then the
+                // inclusive prefix over the lane's rows
+                int tv[R], tf[R], lt = 0;
 #pragma unroll
                 for (int r = 0; r < R; r++) {
-                    int tv = 0, tf = 0;
+                    tv[r] = tf[r] = 0;
                     if (r >= 1 && realx && cs[r] != 0u && !(p.xhalo && xs == 0)) {
                         if (bv[r] - V0 + nvs[r] > p.verts_cap || bf[r] - F0 + nfs[r] > p.faces_cap) {
                             atomicOr(p.err, ERR_CAPACITY);
                         } else {
-                            tv = nvs[r];
-                            tf = nfs[r];
+                            tv[r] = nvs[r];
+                            tf[r] = nfs[r];
                         }
                     }
+                    lt += tv[r] | (tf[r] << 16);
+                }
+                int inc = lt;
 #pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int a = __shfl_up_sync(FULL, tv, o), b = __shfl_up_sync(FULL, tf, o);
-                        if (lane >= o) {
-                            tv += a;
-                            tf += b;
-                        }
-                    }
-                    ws.pv[r * 32 + lane] = (uint16_t)(accv + tv);
-                    ws.pf[r * 32 + lane] = (uint16_t)(accf + tf);
-                    accv += __shfl_sync(FULL, tv, 31);
-                    accf += __shfl_sync(FULL, tf, 31);
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int a = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= o) inc += a;
+                }
+                const int tot = __shfl_sync(FULL, inc, 31);
+                const int accv = tot & 0xffff, accf = tot >> 16;
+                int av = (inc - lt) & 0xffff, af = (inc - lt) >> 16;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    av += tv[r];
+                    af += tf[r];
+                    ws.pv[lane * R + r] = (uint16_t)av;
+                    ws.pf[lane * R + r] = (uint16_t)af;
                 }
                 __syncwarp();
                 const int lo_b = cur ^ 1, hi_b = cur;
@@ -351,7 +380,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                 if (ALG == MESH_ALG_MT) {
                     for (int t = lane; t < accv; t += 32) {
                         const int sc = task_cell(ws.pv, R * 32, t);
-                        const int r = sc >> 5, l = sc & 31;
+                        const int l = sc / R, r = sc - l * R;
                         const int k = t - (sc ? (int)ws.pv[sc - 1] : 0);
                         const unsigned c = ws.cas[cur][r][l];
                         const int xc = x0 + l, yc = y0 - 1 + r;
@@ -391,14 +420,15 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                     // crossing runs with full warps; each lane then adds its cell's
                     // points in edge order from shared memory.
                     NsnPairs &pr = prs[wid];
-                    for (int t0 = 0; t0 < accv; t0 += 32) {
+                    for (int t0 = 0; t0 < accv; t0 += NSN_VC) {
+                        // lanes 0 .. NSN_VC - 1 take the round's cells
                         const int t = t0 + lane;
                         int r = 0, l = 0, n = 0;
                         unsigned crossed = 0;
-                        if (t < accv) {
+                        if (lane < NSN_VC && t < accv) {
                             const int sc = task_cell(ws.pv, R * 32, t);
-                            r = sc >> 5;
-                            l = sc & 31;
+                            l = sc / R;
+                            r = sc - l * R;
                             const unsigned c = ws.cas[cur][r][l];
                             // crossed MC edges as a bit mask (edges 0-7 join corners e, e+1 of
                             // their face ring, 8-11 join e-8 and e-4)
@@ -412,20 +442,24 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                         }
                         int inc = n;
 #pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) {
+                        for (int o = 1; o < NSN_VC; o <<= 1) {
                             const int a = __shfl_up_sync(FULL, inc, o);
                             if (lane >= o) inc += a;
                         }
-                        const int S = __shfl_sync(FULL, inc, 31), beg = inc - n;
-                        pr.end[lane] = inc;
+                        const int S = __shfl_sync(FULL, inc, NSN_VC - 1);
+                        pr.end[lane] = lane < NSN_VC ? inc : S;
                         pr.cell[lane] = crossed | ((unsigned)l << 12) | ((unsigned)r << 17);
+                        const int64_t vq = n ? ws.base[cur][r][l] - V0 : 0;  // this volume's first vertex is 0
                         __syncwarp();
-                        P sum[3] = {P(0), P(0), P(0)};
+                        // the sums: lane 3c + k adds coordinate k of cell c's points in edge order
+                        const int c3 = lane / 3, k3 = lane - 3 * c3;
+                        const int qb3 = c3 < NSN_VC ? pr.end[c3] : 0, qa3 = c3 > 0 && c3 < NSN_VC ? pr.end[c3 - 1] : 0;
+                        P acc = P(0);
                         for (int j0 = 0; j0 < S; j0 += 32) {
                             const int j = j0 + lane;
                             if (j < S) {
-                                // the pair's lane: the first whose inclusive end exceeds j
-                                int lo = 0, hi = 31;
+                                // the pair's cell: the first lane whose inclusive end exceeds j
+                                int lo = 0, hi = NSN_VC - 1;
                                 while (lo < hi) {
                                     const int mid = (lo + hi) >> 1;
                                     if (pr.end[mid] > j) hi = mid;
@@ -446,31 +480,29 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                                 pr.pt[lane][2] = (double)q[2];
                             }
                             __syncwarp();
-                            const int qa = max(beg, j0), qb = min(inc, j0 + 32);
-                            for (int qq = qa; qq < qb; qq++) {
-#pragma unroll
-                                for (int kk = 0; kk < 3; kk++) sum[kk] = Ar<P>::add(sum[kk], (P)pr.pt[qq - j0][kk]);
-                            }
+                            const int qa = max(qa3, j0), qb = min(qb3, j0 + 32);
+                            for (int qq = qa; qq < qb; qq++) acc = Ar<P>::add(acc, (P)pr.pt[qq - j0][k3]);
                             __syncwarp();
                         }
-                        // lanes 0 .. m - 1 hold finished sums: queue them, dividing 32
-                        // at a time (the lanes past the queue's room wait for the flush)
-                        const int m = min(32, accv - t0);
-                        const int64_t vq = t < accv ? ws.base[cur][r][l] - V0 : 0;  // this volume's first vertex is 0
+                        // queue the round's m finished cells (lanes 3c + k hold cell c's sums),
+                        // dividing 32 at a time; cells past the queue's room wait for the flush
+                        const int m = min(NSN_VC, accv - t0);
+                        const long long vq3 = __shfl_sync(FULL, (long long)vq, c3 < NSN_VC ? c3 : 0);
+                        const int n3 = __shfl_sync(FULL, n, c3 < NSN_VC ? c3 : 0);
                         auto push = [&](bool mine, int slot) {
                             if (mine) {
-                                pr.qs[slot][0] = (double)sum[0];
-                                pr.qs[slot][1] = (double)sum[1];
-                                pr.qs[slot][2] = (double)sum[2];
-                                pr.qv[slot] = vq;
-                                pr.qn[slot] = (uint8_t)n;
+                                pr.qs[slot][k3] = (double)acc;
+                                if (k3 == 0) {
+                                    pr.qv[slot] = vq3;
+                                    pr.qn[slot] = (uint8_t)n3;
+                                }
                             }
                         };
-                        push(lane < m && qcount + lane < 32, qcount + lane);
+                        push(c3 < m && qcount + c3 < 32, qcount + c3);
                         if (qcount + m >= 32) {
                             __syncwarp();
                             nsn_means(32);
-                            push(lane < m && qcount + lane >= 32, qcount + lane - 32);
+                            push(c3 < m && qcount + c3 >= 32, qcount + c3 - 32);
                             qcount -= 32;
                         }
                         qcount += m;
@@ -480,7 +512,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                 // faces
                 for (int t = lane; t < accf; t += 32) {
                     const int sc = task_cell(ws.pf, R * 32, t);
-                    const int r = sc >> 5, l = sc & 31;
+                    const int l = sc / R, r = sc - l * R;
                     const int f = t - (sc ? (int)ws.pf[sc - 1] : 0);
                     const unsigned c = ws.cas[cur][r][l];
                     const int xc = x0 + l, yc = y0 - 1 + r;
