@@ -50,6 +50,8 @@ struct MtTables {
     uint8_t za[19];          // axes on which both corners of the edge are 0
     uint8_t shifted[19][8];  // the same lattice edge seen from the cell shifted by -s
     uint8_t kth0[256][MT_MAX_TOUCH];  // interior cells: the k-th owned edge in first-use order
+    uint8_t rank0[256][19];           // interior cells: rank of edge e among the owned edges
+    uint32_t mtw[256];  // by MC case: MT case | interior vertex count << 8 | face count << 13
 };
 
 // One warp's state of a z step.
@@ -144,6 +146,19 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
     HaloWarp<T> *ws_all = reinterpret_cast<HaloWarp<T> *>(smem);
     MtTables *tb = reinterpret_cast<MtTables *>(smem + sizeof(HaloWarp<T>) * WARPS);  // MT
     NsnPairs *prs = reinterpret_cast<NsnPairs *>(smem + sizeof(HaloWarp<T>) * WARPS);  // NSN
+    __shared__ uint16_t s_cross[256];  // NSN: the crossed MC edges of each MC case
+    if (ALG == MESH_ALG_NSN) {
+        for (int c = threadIdx.x; c < 256; c += blockDim.x) {
+            // edges 0-7 join corners e, e+1 of their face ring, 8-11 join e-8 and e-4
+            unsigned m = 0;
+            for (int e = 0; e < 12; e++) {
+                const int ea = e < 8 ? (e & 3) + (e & 4) : e - 8;
+                const int eb = e < 8 ? ((e + 1) & 3) + (e & 4) : e - 4;
+                m |= (((c >> ea) ^ (c >> eb)) & 1u) << e;
+            }
+            s_cross[c] = (uint16_t)m;
+        }
+    }
     if (ALG == MESH_ALG_MT) {
         for (int i = threadIdx.x; i < 256; i += blockDim.x) {
             for (int k = 0; k < 3 * MT_MAX_FACES; k++) tb->faces[i][k] = MT_CASE_FACES[i][k];
@@ -155,6 +170,13 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                 const int ee = MT_TOUCH_ORDER[i][k];
                 if ((p.own[0] >> ee) & 1u) tb->kth0[i][seen++] = (uint8_t)ee;
             }
+            for (int e = 0; e < 19; e++) tb->rank0[i][e] = (uint8_t)__popc(MT_BEFORE[i][e] & p.own[0]);
+            // MC case i -> its corner fields a, b, c, d (the inverse of mc_case) -> the MT case
+            const unsigned a = (i & 1u) | (((i >> 1) & 1u) << 1), b = ((i >> 3) & 1u) | (((i >> 2) & 1u) << 1);
+            const unsigned c = ((i >> 4) & 1u) | (((i >> 5) & 1u) << 1), d = ((i >> 7) & 1u) | (((i >> 6) & 1u) << 1);
+            const unsigned mt = mt_case(a, b, c, d);
+            tb->mtw[i] = mt | ((unsigned)__popc(MT_TOUCHED[mt] & p.own[0] & 0x7ffffu) << 8) |
+                         ((unsigned)MT_CASE_NFACES[mt] << 13);
         }
         if (threadIdx.x < 19) {
             const int e = threadIdx.x;
@@ -253,10 +275,11 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
         if (!cellok[r] || cm == 0u || cm == 255u) return;
         const int yc = y0 - 1 + r;
         if (ALG == MESH_ALG_MT) {
-            cs = mt_case(a, b, c, d);
+            const unsigned w = tb->mtw[cm];
+            cs = w & 255u;
+            nf = (int)(w >> 13);
             const int bnd = (xs + p.xg0 == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
-            nv = __popc(tb->touched[cs] & p.own[bnd] & 0x7ffffu);
-            nf = tb->nfaces[cs];
+            nv = bnd == 0 ? (int)((w >> 8) & 31u) : __popc(tb->touched[cs] & p.own[bnd] & 0x7ffffu);
         } else {
             cs = cm;
             nv = 1;
@@ -429,15 +452,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                             const int sc = task_cell(ws.pv, R * 32, t);
                             l = sc / R;
                             r = sc - l * R;
-                            const unsigned c = ws.cas[cur][r][l];
-                            // crossed MC edges as a bit mask (edges 0-7 join corners e, e+1 of
-                            // their face ring, 8-11 join e-8 and e-4)
-#pragma unroll
-                            for (int e = 0; e < 12; e++) {
-                                const int ea = e < 8 ? (e & 3) + (e & 4) : e - 8;
-                                const int eb = e < 8 ? ((e + 1) & 3) + (e & 4) : e - 4;
-                                crossed |= (((c >> ea) ^ (c >> eb)) & 1u) << e;
-                            }
+                            crossed = s_cross[ws.cas[cur][r][l]];
                             n = __popc(crossed);
                         }
                         int inc = n;
@@ -527,7 +542,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                             const int e = tb->faces[c][3 * f + j];
                             const int sh = tb->za[e] & ~bnd;
                             if (sh == 0) {
-                                id[j] = vb + __popc(__ldg(&MT_BEFORE[c][e]) & own) + 1;
+                                id[j] = vb + (bnd == 0 ? (int)tb->rank0[c][e] : __popc(__ldg(&MT_BEFORE[c][e]) & own)) + 1;
                             } else {
                                 // owned by the neighbour one step back along the axes of sh
                                 const int e2 = tb->shifted[e][sh];
@@ -537,7 +552,8 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                                 const int64_t base2 = ws.base[b2][r2][l2] - V0;
                                 const int bnd2 = ((xc - (sh & 1) + p.xg0) == 0) | (((yc - ((sh >> 1) & 1)) == 0) << 1) |
                                                  (((zc - ((sh >> 2) & 1)) == 0) << 2);
-                                id[j] = base2 + __popc(__ldg(&MT_BEFORE[c2][e2]) & p.own[bnd2]) + 1;
+                                id[j] = base2 +
+                                        (bnd2 == 0 ? (int)tb->rank0[c2][e2] : __popc(__ldg(&MT_BEFORE[c2][e2]) & p.own[bnd2])) + 1;
                             }
                         }
                         o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
