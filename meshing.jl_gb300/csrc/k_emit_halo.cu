@@ -443,8 +443,9 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                     // crossing runs with full warps; each lane then adds its cell's
                     // points in edge order from shared memory.
                     NsnPairs &pr = prs[wid];
-                    for (int t0 = 0; t0 < accv; t0 += NSN_VC) {
-                        // lanes 0 .. NSN_VC - 1 take the round's cells
+                    for (int t0 = 0; t0 < accv;) {
+                        // lanes 0 .. NSN_VC - 1 take the next cells; the round keeps those whose
+                        // pairs fit one sub-round of 32 (at least one cell: a cell has <= 12)
                         const int t = t0 + lane;
                         int r = 0, l = 0, n = 0;
                         unsigned crossed = 0;
@@ -461,14 +462,16 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                             const int a = __shfl_up_sync(FULL, inc, o);
                             if (lane >= o) inc += a;
                         }
-                        const int S = __shfl_sync(FULL, inc, NSN_VC - 1);
-                        pr.end[lane] = lane < NSN_VC ? inc : S;
+                        const int mr = max(1, __popc(__ballot_sync(FULL, lane < NSN_VC && t < accv && inc <= 32)));
+                        const int S = __shfl_sync(FULL, inc, mr - 1);
+                        if (lane >= mr) n = 0;
+                        pr.end[lane] = lane < mr ? inc : S;
                         pr.cell[lane] = crossed | ((unsigned)l << 12) | ((unsigned)r << 17);
                         const int64_t vq = n ? ws.base[cur][r][l] - V0 : 0;  // this volume's first vertex is 0
                         __syncwarp();
                         // the sums: lane 3c + k adds coordinate k of cell c's points in edge order
                         const int c3 = lane / 3, k3 = lane - 3 * c3;
-                        const int qb3 = c3 < NSN_VC ? pr.end[c3] : 0, qa3 = c3 > 0 && c3 < NSN_VC ? pr.end[c3 - 1] : 0;
+                        const int qb3 = c3 < mr ? pr.end[c3] : 0, qa3 = c3 > 0 && c3 < mr ? pr.end[c3 - 1] : 0;
                         P acc = P(0);
                         for (int j0 = 0; j0 < S; j0 += 32) {
                             const int j = j0 + lane;
@@ -501,7 +504,8 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                         }
                         // queue the round's m finished cells (lanes 3c + k hold cell c's sums),
                         // dividing 32 at a time; cells past the queue's room wait for the flush
-                        const int m = min(NSN_VC, accv - t0);
+                        const int m = mr;
+                        t0 += mr;
                         const long long vq3 = __shfl_sync(FULL, (long long)vq, c3 < NSN_VC ? c3 : 0);
                         const int n3 = __shfl_sync(FULL, n, c3 < NSN_VC ? c3 : 0);
                         auto push = [&](bool mine, int slot) {
