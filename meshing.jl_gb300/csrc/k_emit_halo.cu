@@ -96,12 +96,6 @@ __device__ __forceinline__ unsigned mt_case(unsigned a, unsigned b, unsigned c, 
 }
 
 
-template <class A> __device__ __forceinline__ bool is_zero(A v);
-template <> __device__ __forceinline__ bool is_zero<float>(float v) { return (__float_as_uint(v) << 1) == 0u; }
-template <> __device__ __forceinline__ bool is_zero<double>(double v) {
-    return ((unsigned long long)__double_as_longlong(v) << 1) == 0ull;
-}
-
 // c1*b + c2*a in A, with the corner coordinates c1, c2 in {0, 1} and a, b not
 // NaN: the products are b or a (times 1) and zeros carrying the sign of b or a
 // (times 0), so the sum is ab = b + a (both 1), or one term plus a zero -- the
@@ -109,8 +103,8 @@ template <> __device__ __forceinline__ bool is_zero<double>(double v) {
 template <class A> __device__ __forceinline__ A corner_mix(int c1, int c2, A b, A a, A ab) {
     if (c1 && c2) return ab;
     const A t1 = c1 ? b : copysign(A(0), b), t2 = c2 ? a : copysign(A(0), a);
-    if (!is_zero<A>(t1)) return t1;  // t2 is a zero
-    if (!is_zero<A>(t2)) return t2;
+    if (!bits_zero(t1)) return t1;  // t2 is a zero
+    if (!bits_zero(t2)) return t2;
     return (signbit(t1) && signbit(t2)) ? -A(0) : A(0);
 }
 
@@ -124,7 +118,7 @@ __device__ __forceinline__ void mt_point(const Plan &p, int e, int x, int y, int
     const A hi = sizeof(A) == 4 ? (A)p.hi_f : (A)p.hi_d;
     const A a = jl_min<A>(jl_max<A>((A)q, eps), hi);
     const A b = Ar<A>::sub(A(1), a);
-    const bool nan = isnan(a);  // then b and every weight are NaN
+    const bool nan = bits_nan(a);  // then b and every weight are NaN
     const A ab = Ar<A>::add(b, a);
     const int idx[3] = {x, y, z};
     const double *tp[3] = {p.xp, p.yp, p.zp};

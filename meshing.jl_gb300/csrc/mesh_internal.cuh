@@ -330,15 +330,28 @@ template <class Q, class T> __device__ __forceinline__ Q quotient(T v1, T v2, co
     return Ar<Q>::div(num, den);
 }
 
+// Classification of IEEE values by their bits, so that Float64 tests stay off
+// the (1/64-rate) FP64 pipe.
+__device__ __forceinline__ bool bits_nan(float v) { return (__float_as_uint(v) << 1) > 0xff000000u; }
+__device__ __forceinline__ bool bits_nan(double v) {
+    return ((unsigned long long)__double_as_longlong(v) << 1) > 0xffe0000000000000ull;
+}
+__device__ __forceinline__ bool bits_finite(float v) { return (__float_as_uint(v) << 1) < 0xff000000u; }
+__device__ __forceinline__ bool bits_finite(double v) {
+    return ((unsigned long long)__double_as_longlong(v) << 1) < 0xffe0000000000000ull;
+}
+__device__ __forceinline__ bool bits_zero(float v) { return (__float_as_uint(v) << 1) == 0u; }
+__device__ __forceinline__ bool bits_zero(double v) { return ((unsigned long long)__double_as_longlong(v) << 1) == 0ull; }
+
 // Base.max / Base.min on IEEE floats: NaN propagates, -0.0 < +0.0.
 template <class A> __device__ __forceinline__ A jl_max(A x, A y) {
     A d = Ar<A>::sub(x, y);
-    if (isnan(x) || isnan(y)) return d;
+    if (bits_nan(x) || bits_nan(y)) return d;
     return signbit(d) ? y : x;
 }
 template <class A> __device__ __forceinline__ A jl_min(A x, A y) {
     A d = Ar<A>::sub(x, y);
-    if (isnan(x) || isnan(y)) return d;
+    if (bits_nan(x) || bits_nan(y)) return d;
     return signbit(d) ? x : y;
 }
 

@@ -12,7 +12,7 @@ template <> __device__ __forceinline__ float tab<float>(const double *, const fl
 
 // Coordinate on an axis the edge does not move along: p1 + mu*(p1 - p1).
 template <class P> __device__ __forceinline__ P still(P c, P mu) {
-    if (c != P(0) && isfinite(mu)) return c;
+    if (!bits_zero(c) && bits_finite(mu)) return c;
     return Ar<P>::add(c, Ar<P>::mul(mu, P(0)));
 }
 
