@@ -73,6 +73,7 @@ struct NsnPairs {
     double qs[32][3];
     long long qv[32];
     uint8_t qn[32];
+    uint8_t tcell[R * 32];  // the step's vertex task t (one per active cell) -> its cell lane * R + row
 };
 
 // First entry of the inclusive prefix a[0..n) above t (a[n-1] > t).
@@ -390,6 +391,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                     af += tf[r];
                     ws.pv[lane * R + r] = (uint16_t)av;
                     ws.pf[lane * R + r] = (uint16_t)af;
+                    if (ALG == MESH_ALG_NSN && tv[r]) prs[wid].tcell[av - 1] = (uint8_t)(lane * R + r);
                 }
                 __syncwarp();
                 const int lo_b = cur ^ 1, hi_b = cur;
@@ -444,7 +446,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                         int r = 0, l = 0, n = 0;
                         unsigned crossed = 0;
                         if (lane < NSN_VC && t < accv) {
-                            const int sc = task_cell(ws.pv, R * 32, t);
+                            const int sc = pr.tcell[t];
                             l = sc / R;
                             r = sc - l * R;
                             crossed = s_cross[ws.cas[cur][r][l]];
