@@ -44,8 +44,6 @@ constexpr int NSN_VC = 10; // NSN: cells per vertex round (three lanes per cell 
 
 struct MtTables {
     uint8_t faces[256][3 * MT_MAX_FACES];
-    uint8_t order[256][MT_MAX_TOUCH];
-    uint32_t touched[256];
     uint8_t nfaces[256];
     uint8_t za[19];          // axes on which both corners of the edge are 0
     uint8_t shifted[19][8];  // the same lattice edge seen from the cell shifted by -s
@@ -63,11 +61,9 @@ template <class T> struct HaloWarp {
     uint16_t pv[R * 32], pf[R * 32];  // inclusive prefix of vertex / face tasks over (lane, row)
 };
 
-// NSN: one round of up to 32 vertex tasks as (cell, crossed edge) pairs.
+// NSN: a round of vertex tasks as (cell, crossed edge) pairs.
 struct NsnPairs {
-    int end[32];         // inclusive prefix of the round's lanes' pair counts
-    uint32_t cell[32];   // crossed-edge mask | lane << 12 | row << 17 of the lane's cell
-    double pt[32][3];    // crossing points of a sub-round of 32 pairs
+    double pt[32][3];    // crossing points of the round's (at most 32) pairs
     // vertices whose sums are complete, waiting for their mean: divided 32 at
     // a time, so that the Float64 divisions run with full warps across steps
     double qs[32][3];
@@ -75,6 +71,8 @@ struct NsnPairs {
     uint8_t qn[32];
     uint8_t tcell[R * 32];  // the step's vertex task t (one per active cell) -> its cell lane * R + row
 };
+
+__device__ __forceinline__ uint32_t lanemask_le(int lane) { return (2u << lane) - 1u; }
 
 // First entry of the inclusive prefix a[0..n) above t (a[n-1] > t).
 __device__ __forceinline__ int task_cell(const uint16_t *a, int n, int t) {
@@ -157,8 +155,6 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
     if (ALG == MESH_ALG_MT) {
         for (int i = threadIdx.x; i < 256; i += blockDim.x) {
             for (int k = 0; k < 3 * MT_MAX_FACES; k++) tb->faces[i][k] = MT_CASE_FACES[i][k];
-            for (int k = 0; k < MT_MAX_TOUCH; k++) tb->order[i][k] = MT_TOUCH_ORDER[i][k];
-            tb->touched[i] = MT_TOUCHED[i];
             tb->nfaces[i] = MT_CASE_NFACES[i];
             const int nt = __popc(MT_TOUCHED[i]);
             for (int k = 0, seen = 0; k < nt; k++) {
@@ -274,7 +270,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
             cs = w & 255u;
             nf = (int)(w >> 13);
             const int bnd = (xs + p.xg0 == 0) | ((yc == 0) << 1) | ((zc == 0) << 2);
-            nv = bnd == 0 ? (int)((w >> 8) & 31u) : __popc(tb->touched[cs] & p.own[bnd] & 0x7ffffu);
+            nv = bnd == 0 ? (int)((w >> 8) & 31u) : __popc(__ldg(&MT_TOUCHED[cs]) & p.own[bnd] & 0x7ffffu);
         } else {
             cs = cm;
             nv = 1;
@@ -412,9 +408,9 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                         if (bnd == 0) {
                             e = tb->kth0[c][k];
                         } else {
-                            const int nt = __popc(tb->touched[c]);
+                            const int nt = __popc(__ldg(&MT_TOUCHED[c]));
                             for (int i = 0, seen = 0; i < nt; i++) {
-                                const int ee = tb->order[c][i];
+                                const int ee = __ldg(&MT_TOUCH_ORDER[c][i]);
                                 if (!((own >> ee) & 1u)) continue;
                                 if (seen == k) {
                                     e = ee;
@@ -459,45 +455,38 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
                             if (lane >= o) inc += a;
                         }
                         const int mr = max(1, __popc(__ballot_sync(FULL, lane < NSN_VC && t < accv && inc <= 32)));
-                        const int S = __shfl_sync(FULL, inc, mr - 1);
+                        const int S = __shfl_sync(FULL, inc, mr - 1);  // the round's pairs: at most 32
                         if (lane >= mr) n = 0;
-                        pr.end[lane] = lane < mr ? inc : S;
-                        pr.cell[lane] = crossed | ((unsigned)l << 12) | ((unsigned)r << 17);
+                        const int beg = inc - n;  // the cell's first pair
+                        const unsigned cw = crossed | ((unsigned)l << 12) | ((unsigned)r << 17);
                         const int64_t vq = n ? ws.base[cur][r][l] - V0 : 0;  // this volume's first vertex is 0
+                        // pair j = lane: its cell is the last one that begins at or before j
+                        const unsigned starts = __reduce_or_sync(FULL, n ? 1u << beg : 0u);
+                        const int own = max(0, __popc(starts & lanemask_le(lane)) - 1);
+                        const unsigned cwo = __shfl_sync(FULL, cw, own);
+                        const int bego = __shfl_sync(FULL, beg, own);
+                        if (lane < S) {
+                            const int e = (int)__fns(cwo & 0xfffu, 0, lane - bego + 1);
+                            const int r2 = (int)(cwo >> 17), l2 = (int)((cwo >> 12) & 31u);
+                            const McEdge g = mc_edge(e);
+                            const int ca = mc_corner_off(g.a), cb = mc_corner_off(g.b);
+                            const T va = ws.samp[(ca & 4) ? hi_b : lo_b][r2 + ((ca >> 1) & 1)][l2 + (ca & 1)];
+                            const T vbv = ws.samp[(cb & 4) ? hi_b : lo_b][r2 + ((cb >> 1) & 1)][l2 + (cb & 1)];
+                            P q[3];
+                            mc_edge_point<T, Q, P>(p, g, x0 + l2, y0 - 1 + r2, zc, va, vbv, q);
+                            pr.pt[lane][0] = (double)q[0];
+                            pr.pt[lane][1] = (double)q[1];
+                            pr.pt[lane][2] = (double)q[2];
+                        }
                         __syncwarp();
                         // the sums: lane 3c + k adds coordinate k of cell c's points in edge order
                         const int c3 = lane / 3, k3 = lane - 3 * c3;
-                        const int qb3 = c3 < mr ? pr.end[c3] : 0, qa3 = c3 > 0 && c3 < mr ? pr.end[c3 - 1] : 0;
+                        const int src3 = c3 < mr ? c3 : 0;
+                        const int qa3 = __shfl_sync(FULL, beg, src3), qb3 = __shfl_sync(FULL, inc, src3);
                         P acc = P(0);
-                        for (int j0 = 0; j0 < S; j0 += 32) {
-                            const int j = j0 + lane;
-                            if (j < S) {
-                                // the pair's cell: the first lane whose inclusive end exceeds j
-                                int lo = 0, hi = NSN_VC - 1;
-                                while (lo < hi) {
-                                    const int mid = (lo + hi) >> 1;
-                                    if (pr.end[mid] > j) hi = mid;
-                                    else lo = mid + 1;
-                                }
-                                const unsigned cw = pr.cell[lo];
-                                const int k = j - (lo ? pr.end[lo - 1] : 0);
-                                const int e = (int)__fns(cw & 0xfffu, 0, k + 1);
-                                const int r2 = (int)(cw >> 17), l2 = (int)((cw >> 12) & 31u);
-                                const McEdge g = mc_edge(e);
-                                const int ca = mc_corner_off(g.a), cb = mc_corner_off(g.b);
-                                const T va = ws.samp[(ca & 4) ? hi_b : lo_b][r2 + ((ca >> 1) & 1)][l2 + (ca & 1)];
-                                const T vbv = ws.samp[(cb & 4) ? hi_b : lo_b][r2 + ((cb >> 1) & 1)][l2 + (cb & 1)];
-                                P q[3];
-                                mc_edge_point<T, Q, P>(p, g, x0 + l2, y0 - 1 + r2, zc, va, vbv, q);
-                                pr.pt[lane][0] = (double)q[0];
-                                pr.pt[lane][1] = (double)q[1];
-                                pr.pt[lane][2] = (double)q[2];
-                            }
-                            __syncwarp();
-                            const int qa = max(qa3, j0), qb = min(qb3, j0 + 32);
-                            for (int qq = qa; qq < qb; qq++) acc = Ar<P>::add(acc, (P)pr.pt[qq - j0][k3]);
-                            __syncwarp();
-                        }
+                        if (c3 < mr)
+                            for (int qq = qa3; qq < qb3; qq++) acc = Ar<P>::add(acc, (P)pr.pt[qq][k3]);
+                        __syncwarp();
                         // queue the round's m finished cells (lanes 3c + k hold cell c's sums),
                         // dividing 32 at a time; cells past the queue's room wait for the flush
                         const int m = mr;
