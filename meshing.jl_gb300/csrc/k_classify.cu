@@ -646,6 +646,8 @@ __device__ __forceinline__ void tma_mc_consume(const Plan &p, const uint32_t *s_
     uint32_t cv[WY], cf[WY], ca[WY], pk[WY];
 #pragma unroll
     for (int r = 0; r < WY; r++) cv[r] = cf[r] = ca[r] = pk[r] = 0;
+    // per sample row of a plane: the lane's 2-bit field (x, x+1), extracted once per
+    // plane and shared by the two steps that use the plane
     uint32_t mlo[WY + 1], alo = 0, olo = 0;
 
     auto masks = [&](const T *st, int k, uint32_t (&m)[WY + 1], uint32_t &a, uint32_t &o) {
@@ -653,16 +655,17 @@ __device__ __forceinline__ void tma_mc_consume(const Plan &p, const uint32_t *s_
         o = 0;
 #pragma unroll
         for (int r = 0; r <= WY; r++) {
-            m[r] = __ballot_sync(FULL, rowok[r] && below(st[k * PLANE + off[r]], p));
-            a &= m[r];
-            o |= m[r];
+            const uint32_t b = __ballot_sync(FULL, rowok[r] && below(st[k * PLANE + off[r]], p));
+            a &= b;
+            o |= b;
+            m[r] = (b >> lane) & 3u;
         }
     };
     auto step = [&](const uint32_t (&mhi)[WY + 1], uint32_t ahi, uint32_t ohi) {
         if ((alo & ahi) != xval && (olo | ohi) != 0u) {
             uint32_t nb[WY + 1];
 #pragma unroll
-            for (int r = 0; r <= WY; r++) nb[r] = row_field(mlo[r], mhi[r], lane);
+            for (int r = 0; r <= WY; r++) nb[r] = mlo[r] | (mhi[r] << 2);
 #pragma unroll
             for (int r = 0; r < WY; r++) pk[r] += s_tab[nb[r] | (nb[r + 1] << 4)] & rmask[r];
         }
