@@ -291,8 +291,23 @@ __device__ __forceinline__ bool below(int16_t v, const Plan &p) { return (int64_
 __device__ __forceinline__ bool below(int32_t v, const Plan &p) { return (int64_t)v < p.thr_l || p.thr_all; }
 __device__ __forceinline__ bool below(int64_t v, const Plan &p) { return v < p.thr_l || p.thr_all; }
 
+// A Float32 value widened to Q.  To Float64 the widening of a normal or zero
+// value only moves bits (exponent rebiased by 1023 - 127, significand shifted
+// up by 29), done here on the integer pipes; subnormals, Inf and NaN take the
+// conversion instruction.
+template <class Q> __device__ __forceinline__ Q widen(float v) { return (Q)v; }
+template <> __device__ __forceinline__ double widen<double>(float v) {
+    const uint32_t u = __float_as_uint(v), e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e != 0u && e != 0xffu)
+        return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
+                                                ((unsigned long long)(u & 0x7fffffu) << 29)));
+    if ((u << 1) == 0u) return __longlong_as_double((long long)sgn);
+    return (double)v;
+}
+
 // v2 - v1 in the data type (UInt16 wraps), then converted to Q.
-template <class Q> __device__ __forceinline__ Q tdiff(float v2, float v1) { return (Q)__fsub_rn(v2, v1); }
+template <class Q> __device__ __forceinline__ Q tdiff(float v2, float v1) { return widen<Q>(__fsub_rn(v2, v1)); }
 // Float16 - Float16 is a Float16: the Float32 difference of two Float16 values
 // is exact, so rounding it to Float16 once gives the IEEE half subtraction.
 template <class Q> __device__ __forceinline__ Q tdiff(h16 v2, h16 v1) {
@@ -325,6 +340,8 @@ template <class Q, class T> __device__ __forceinline__ Q quotient(T v1, T v2, co
     Q num;
     if (std::is_integral<T>::value && sizeof(T) == 8 && p.iso_int)  // Int64 data, Int64 iso: Int64 (iso - v1)
         num = (Q)(int64_t)((unsigned long long)p.iso_l - (unsigned long long)(int64_t)v1);
+    else if (std::is_same<T, float>::value)
+        num = Ar<Q>::sub(isoq<Q>(p), widen<Q>((float)v1));
     else
         num = Ar<Q>::sub(isoq<Q>(p), (Q)v1);
     return Ar<Q>::div(num, den);
