@@ -18,14 +18,19 @@
 //
 // Tiling: 30 x-cells (lanes 1..30) plus the -x neighbour (lane 0) by WY
 // y-cells plus the -y neighbour row, one z segment; lane 31 only supplies
-// samples.  Warps are persistent and take their tiles from a work counter.  Per z step the warp classifies its cells lane by lane, then
-// stages the step in its shared memory -- the sample values of both planes,
-// the cases and vertex bases of the current and previous plane, each cell's
-// first face -- with the inclusive prefix of the cells' vertex and face
-// counts.  All 32 lanes then work through the step's vertices and faces as
-// dense task lists (task t -> its cell by binary search over the prefix), so
-// a warp instruction serves up to 32 vertices or faces instead of the few
-// active cells of one row.  Neighbour lookups are plain shared loads.
+// samples.  Warps are persistent and take their tiles from a work counter.
+// Per z step the warp classifies its cells lane by lane, then stages the step
+// in its shared memory -- the sample values of both planes, the cases and
+// vertex bases of the current and previous plane, each cell's first face --
+// with the inclusive prefix of the cells' vertex and face counts in (lane,
+// row) order.  All 32 lanes then work through the step's vertices and faces
+// as dense task lists (task t -> its cell by binary search over the prefix;
+// NSN vertices through a per-step table, one vertex per active cell), so a
+// warp instruction serves up to 32 vertices or faces instead of the few
+// active cells of one row.  NSN expands each round of cells into its (cell,
+// crossed edge) pairs so that the Float64 crossing points run with full
+// warps, and divides the means 32 at a time from a per-warp queue.
+// Neighbour lookups are plain shared loads.
 #define MESH_TBL static __device__ const
 #include "mesh_internal.cuh"
 #include "mesh_tables.h"
