@@ -179,6 +179,24 @@ def test_nan_inf_ties_and_signed_zero(pkg, oracle, cuda, alg):
 
 
 @pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
+def test_float32_subnormal_tiny_and_huge_samples_with_a_float64_iso(pkg, oracle, cuda, alg):
+    # Float32 samples widened to the Float64 quotient type: normal values move
+    # their bits, zeros keep their sign, subnormals / Inf / NaN take the
+    # conversion instruction; every kind next to every other
+    rng = np.random.default_rng(23)
+    kinds = np.array([1e-45, -1e-45, 3e-42, -2.5e-40, 1.1754942e-38, -1.17549435e-38, 1.2e-38, 0.0, -0.0,
+                      3.0e38, -3.4028235e38, 1.0, -1.0, 0.5, np.inf, -np.inf, np.nan], dtype=np.float32)
+    A = kinds[rng.integers(0, len(kinds), (13, 12, 14))]
+    for iso in (0.0, 1e-40, -2e-39, 1.0000000000000002):
+        check(pkg, oracle, A, alg, iso)
+    check(pkg, oracle, A, alg, 0.0, 1e-3, ((-1.0, 1.0), (0.0, 2.0), (-3.0, 0.0)), device=True)
+    if alg == 'mc':
+        A = np.asfortranarray(A)
+        m = pkg.MarchingCubes(iso=1e-40, weld=True)
+        assert_same(pkg.isosurface(A, m), oracle.isosurface(A, 'mcw', 1e-40), 'welded, special Float32 samples')
+
+
+@pytest.mark.parametrize('alg', ['mc', 'mt', 'nsn'])
 def test_uint16_wraparound(pkg, oracle, cuda, alg):
     rng = np.random.default_rng(5)
     A = np.where(rng.random((20, 21, 22)) < 0.5, rng.integers(0, 400, (20, 21, 22)),
