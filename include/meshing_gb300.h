@@ -208,14 +208,19 @@ MESH_API int mesh_extract_noalloc(const void *vol, int vol_dtype, int64_t nx, in
 typedef struct mesh_batch mesh_batch;
 /* n volumes of dtype `vol_dtype` in device memory (Julia layout), vols[i] with
  * sizes dims[3i..3i+2], extracted with the MarchingCubes parameters p
- * (p->alg must be MESH_ALG_MC).  ranges: n x 6 endpoints (x0 x1 y0 y1 z0 z1,
+ * (p->alg MESH_ALG_MC, or MESH_ALG_MC_WELDED for every volume's welded mesh:
+ * the per-cell meshes are welded with edge keys made distinct per volume, and
+ * the outputs, faces and rows below are the welded ones).  ranges: n x 6 endpoints (x0 x1 y0 y1 z0 z1,
  * of p->range_type), or NULL for p->range on every volume.  Pointers and sizes
  * are fixed for the batch's lifetime; the volumes' contents may change. */
 MESH_API int mesh_batch_create(mesh_ctx *ctx, int n, const void *const *vols, int vol_dtype, const int64_t *dims,
                                const mesh_params *p, const double *ranges, mesh_batch **out);
 MESH_API void mesh_batch_destroy(mesh_batch *b);
 /* Classifies and scans every volume (waits for the result) and sizes the
- * batch's outputs exactly: total vertices and faces. */
+ * batch's outputs exactly: total vertices and faces.  Welded batches run the
+ * whole extraction and weld once here, so that the welded vertices are sized
+ * exactly as well; later runs on changed contents report their welded rows in
+ * the offsets. */
 MESH_API int mesh_batch_count(mesh_batch *b, int64_t *nverts, int64_t *nfaces);
 /* Queues the whole extraction into the batch's outputs; with graphs enabled it
  * is captured once into a CUDA graph and replayed.  Outputs larger than at the

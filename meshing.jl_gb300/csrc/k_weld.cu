@@ -66,8 +66,11 @@ __device__ __forceinline__ long long cta_scan(long long v, long long *s_w, long 
     return r;
 }
 
-__global__ void __launch_bounds__(WT) k_weld_count(const long long *vkey, int64_t nv, long long *bsum) {
+// dev_nv (batches): the vertex count, read on the device, at most nv
+__global__ void __launch_bounds__(WT) k_weld_count(const long long *vkey, int64_t nv, long long *bsum,
+                                                   const int64_t *dev_nv = nullptr) {
     __shared__ long long s_w[33];
+    if (dev_nv) nv = min(nv, dev_nv[0]);
     const int64_t v0 = (int64_t)blockIdx.x * WB + (int64_t)threadIdx.x * WPT;
     long long c = 0;
 #pragma unroll
@@ -99,8 +102,10 @@ __global__ void __launch_bounds__(1024) k_weld_scan(long long *bsum, int64_t nb)
 template <class F>
 __global__ void __launch_bounds__(WT) k_weld_place(const long long *vkey, int64_t nv, const long long *bsum,
                                                    const F *verts, F *wverts, unsigned long long *hkey,
-                                                   long long *hval, int64_t hcap, unsigned *err) {
+                                                   long long *hval, int64_t hcap, unsigned *err,
+                                                   const int64_t *dev_nv = nullptr) {
     __shared__ long long s_w[33];
+    if (dev_nv) nv = min(nv, dev_nv[0]);
     const int64_t v0 = (int64_t)blockIdx.x * WB + (int64_t)threadIdx.x * WPT;
     long long c = 0;
 #pragma unroll
@@ -163,6 +168,72 @@ __global__ void __launch_bounds__(WT) k_weld_faces(const long long *vkey, int64_
     }
 }
 
+// Batches: the welded first vertex of every volume v (row n: the welded total)
+// is the number of owned vertices before its first ordinary vertex -- the
+// scanned count of its block plus the owned vertices of that block before it
+// (a warp per volume); the face rows are unchanged.
+__global__ void __launch_bounds__(256) k_weld_vol_offsets(const long long *vkey, int64_t nvmax, const int64_t *tot,
+                                                          const long long *bsum, const int64_t *vol_off, int n,
+                                                          int64_t *woff) {
+    const int lane = threadIdx.x & 31;
+    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (v > n) return;  // warp-uniform
+    const int64_t nv = min(nvmax, tot[0]);
+    const int64_t i = min(nv, vol_off[2 * v]);
+    const int64_t b0 = (i / WB) * WB;
+    long long c = 0;
+    for (int64_t j = b0 + lane; j < i; j += 32) c += vkey[j] < 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL, c, o);
+    if (lane == 0) {
+        woff[2 * v] = bsum[i / WB] + c;
+        woff[2 * v + 1] = vol_off[2 * v + 1];
+    }
+}
+
+// Batches: every face vertex (1-based within its volume) becomes the welded
+// vertex of its edge, 1-based within the volume's welded vertices.  A face's
+// volume is the last one whose first face is at or before it (volumes without
+// faces share their successor's first face).
+__global__ void __launch_bounds__(WT) k_weld_faces_batch(const long long *vkey, int64_t nvmax, int64_t nfmax,
+                                                         const int64_t *tot, int64_t *faces, const int64_t *vol_off,
+                                                         const int64_t *woff, int n,
+                                                         const unsigned long long *hkey, const long long *hval,
+                                                         int64_t hcap, unsigned *err) {
+    const int64_t nv = min(nvmax, tot[0]), m = 3 * min(nfmax, tot[1]);
+    const unsigned long long mask = (unsigned long long)hcap - 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = i / 3;
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (vol_off[2 * mid + 1] <= f) lo = mid;
+            else hi = mid - 1;
+        }
+        const int64_t j = vol_off[2 * lo] + faces[i] - 1;
+        if (j < 0 || j >= nv) {
+            atomicOr(err, ERR_BOUNDS);
+            continue;
+        }
+        const unsigned long long key = (unsigned long long)(vkey[j] & ~OWN) + 1;
+        unsigned long long h = mix64(key) & mask;
+        long long id = -1;
+        for (int64_t probe = 0; probe < hcap; probe++, h = (h + 1) & mask) {
+            const unsigned long long k = hkey[h];
+            if (k == key) {
+                id = hval[h];
+                break;
+            }
+            if (k == 0ull) break;
+        }
+        if (id < 0) {
+            atomicOr(err, ERR_BOUNDS);
+            continue;
+        }
+        faces[i] = id - woff[2 * lo] + 1;
+    }
+}
+
 }  // namespace
 
 // Hash slots for nv ordinary vertices (a power of two, at least twice the
@@ -194,6 +265,33 @@ cudaError_t launch_weld(const long long *vkey, int64_t nv, const void *verts, in
     if (n > 0)
         k_weld_faces<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n + WT - 1) / WT, (int64_t)sms * 16)), WT,
                        0, s>>>(vkey, nv, faces, n, hkey, hval, hcap, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weld_batch(const long long *vkey, int64_t nvmax, int64_t nfmax, const int64_t *tot,
+                              const void *verts, int out64, int64_t *faces, const int64_t *vol_off, int n,
+                              int64_t *woff, long long *bsum, void *wverts, unsigned long long *hkey, long long *hval,
+                              int64_t hcap, unsigned *err, int sms, cudaStream_t s) {
+    const int64_t nb = weld_blocks(nvmax);
+    cudaError_t e = cudaMemsetAsync(hkey, 0, (size_t)hcap * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bsum, 0, (size_t)(nb + 1) * sizeof(long long), s);
+    if (e != cudaSuccess) return e;
+    if (nb > 0) {
+        k_weld_count<<<(unsigned)nb, WT, 0, s>>>(vkey, nvmax, bsum, tot);
+        k_weld_scan<<<1, 1024, 0, s>>>(bsum, nb);
+        if (out64)
+            k_weld_place<double><<<(unsigned)nb, WT, 0, s>>>(vkey, nvmax, bsum, (const double *)verts,
+                                                             (double *)wverts, hkey, hval, hcap, err, tot);
+        else
+            k_weld_place<float><<<(unsigned)nb, WT, 0, s>>>(vkey, nvmax, bsum, (const float *)verts,
+                                                            (float *)wverts, hkey, hval, hcap, err, tot);
+    }
+    k_weld_vol_offsets<<<(unsigned)((32 * ((int64_t)n + 1) + 255) / 256), 256, 0, s>>>(vkey, nvmax, tot, bsum, vol_off,
+                                                                                      n, woff);
+    const int64_t m = 3 * nfmax;
+    if (m > 0 && n > 0)
+        k_weld_faces_batch<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((m + WT - 1) / WT, (int64_t)sms * 16)),
+                             WT, 0, s>>>(vkey, nvmax, nfmax, tot, faces, vol_off, woff, n, hkey, hval, hcap, err);
     return cudaGetLastError();
 }
 

@@ -48,6 +48,12 @@ struct mesh_batch {
     int64_t nverts = 0, nfaces = 0, nactive = 0;
     int counted = 0;
     int use_graph = 0;
+    // welded batches: the per-cell mesh goes to out_v / out_f, its edge keys to
+    // wkey; the welded vertices to wv, the faces are renumbered in place, the
+    // welded rows to woffs
+    int weld = 0;
+    int64_t nv_cell = 0;          // per-cell vertices at the last count
+    DevBuf wkey, wbuf, wv, woffs;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t cap = nullptr;   // capture stream (the legacy default stream cannot be captured)
 };
@@ -63,6 +69,8 @@ BatchSizes tile_batch(const int64_t *dims, int n, int zs, std::vector<BatchVol> 
         const int64_t nx = dims[3 * v], ny = dims[3 * v + 1], nz = dims[3 * v + 2];
         bv.nx = nx; bv.ny = ny; bv.nz = nz;
         bv.item0 = z.items; bv.piece0 = z.pieces; bv.flag0 = z.nflags; bv.stile0 = (int32_t)z.stiles;
+        bv.kbase = z.keys;
+        z.keys += 3 * nx * ny * nz;
         tab_off[v] = z.tdoubles;
         if (nx < 2 || ny < 2 || nz < 2) {  // no cells: an empty mesh
             bv.zs = ZC; bv.chunks_per_seg = 1;
@@ -220,6 +228,17 @@ int enqueue_run(mesh_batch *b, cudaStream_t s) {
     cudaError_t e;
     if ((e = launch_compact_batch(b->P, b->cmp_ctas, s)) != cudaSuccess) return cuda_fail(c, e, "batch compact");
     if ((e = launch_expand_batch(b->P, b->Q64, b->P64, s)) != cudaSuccess) return cuda_fail(c, e, "batch expand");
+    if (b->weld) {
+        const Plan &P = b->P;
+        const int64_t nb = weld_blocks(b->nv_cell), hcap = weld_hash_slots(b->nv_cell);
+        char *wb = (char *)b->wbuf.ptr;
+        const size_t o_hkey = ((size_t)(nb + 1) * 8 + 255) / 256 * 256, o_hval = o_hkey + (size_t)hcap * 8;
+        if ((e = launch_weld_batch(P.vkey, b->nv_cell, b->nfaces, P.totals, P.verts, P.out64, P.faces, P.vol_off, b->n,
+                                   (int64_t *)b->woffs.ptr, (long long *)wb, b->wv.ptr,
+                                   (unsigned long long *)(wb + o_hkey), (long long *)(wb + o_hval), hcap, P.err,
+                                   c->sms, s)) != cudaSuccess)
+            return cuda_fail(c, e, "batch weld");
+    }
     return MESH_OK;
 }
 
@@ -256,7 +275,24 @@ int count(mesh_batch *b) {
     P.faces = (int64_t *)b->out_f.ptr;
     P.verts_cap = b->nverts;
     P.faces_cap = b->nfaces;
+    P.vkey = nullptr;
     b->counted = 1;
+    if (!b->weld) return MESH_OK;
+    // welded: edge keys, weld scratch, welded vertices and rows; one whole run
+    // (per-cell mesh and weld) sizes the welded vertices exactly
+    b->nv_cell = b->nverts;
+    const int64_t nb = weld_blocks(b->nv_cell), hcap = weld_hash_slots(b->nv_cell);
+    const size_t wbytes = up((size_t)(nb + 1) * 8) + (size_t)hcap * 16;
+    if ((e = b->wkey.ensure((size_t)b->nv_cell * 8 + 16)) != cudaSuccess || (e = b->wbuf.ensure(wbytes)) != cudaSuccess ||
+        (e = b->wv.ensure(vb + 16)) != cudaSuccess || (e = b->woffs.ensure((size_t)(b->n + 1) * 16)) != cudaSuccess)
+        return cuda_fail(c, e, "weld buffers");
+    P.vkey = (long long *)b->wkey.ptr;
+    if ((rc = enqueue_run(b, c->stream)) || (rc = fetch(b))) return rc;
+    int64_t row[2];
+    if ((e = cudaMemcpy(row, (int64_t *)b->woffs.ptr + 2 * (size_t)b->n, sizeof(row), cudaMemcpyDeviceToHost)) !=
+        cudaSuccess)
+        return cuda_fail(c, e, "welded totals");
+    b->nverts = row[0];
     return MESH_OK;
 }
 
@@ -325,7 +361,8 @@ int mesh_batch_create(mesh_ctx *ctx, int n, const void *const *vols, int dtype, 
     *out = nullptr;
     ctx->msg.clear();
     if (!p) return fail(ctx, MESH_EINVAL, "params is NULL");
-    if (p->alg != MESH_ALG_MC) return fail(ctx, MESH_EINVAL, "batches run MarchingCubes only");
+    if (p->alg != MESH_ALG_MC && p->alg != MESH_ALG_MC_WELDED)
+        return fail(ctx, MESH_EINVAL, "batches run MarchingCubes only");
     for (int v = 0; v < n; v++) {
         mesh_params q = *p;
         if (ranges) memcpy(q.range, ranges + 6 * v, sizeof(q.range));
@@ -341,6 +378,8 @@ int mesh_batch_create(mesh_ctx *ctx, int n, const void *const *vols, int dtype, 
     b->n = n;
     b->T = dtype;
     b->prm = *p;
+    b->weld = p->alg == MESH_ALG_MC_WELDED;
+    b->prm.alg = MESH_ALG_MC;  // welded batches run the Marching Cubes kernels, then weld
     b->vols.assign(vols, vols + n);
     b->dims.assign(dims, dims + 3 * n);
     b->ranges.resize(6 * (size_t)n);
@@ -365,8 +404,8 @@ void mesh_batch_destroy(mesh_batch *b) {
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     drop_graph(b);
-    DevBuf *bufs[] = {&b->dvols, &b->ivol, &b->svol, &b->tabs, &b->jobs, &b->cnt, &b->base, &b->flags,
-                      &b->scan,  &b->misc, &b->ent,  &b->out_v, &b->out_f, &b->offs};
+    DevBuf *bufs[] = {&b->dvols, &b->ivol, &b->svol,  &b->tabs, &b->jobs, &b->cnt,  &b->base, &b->flags, &b->scan,
+                      &b->misc,  &b->ent,  &b->out_v, &b->out_f, &b->offs, &b->wkey, &b->wbuf, &b->wv,   &b->woffs};
     for (DevBuf *x : bufs) x->release();
     if (b->h_misc) cudaFreeHost(b->h_misc);
     if (b->cap) cudaStreamDestroy(b->cap);
@@ -399,9 +438,9 @@ int mesh_batch_sync(mesh_batch *b) {
 int mesh_batch_outputs(mesh_batch *b, void **verts, int64_t **faces, int64_t **offsets) {
     if (!b || !verts || !faces || !offsets) return MESH_EINVAL;
     if (!b->counted) return fail(b->ctx, MESH_ESTATE, "mesh_batch_outputs without mesh_batch_count");
-    *verts = b->out_v.ptr;
+    *verts = b->weld ? b->wv.ptr : b->out_v.ptr;
     *faces = (int64_t *)b->out_f.ptr;
-    *offsets = (int64_t *)b->offs.ptr;
+    *offsets = (int64_t *)(b->weld ? b->woffs.ptr : b->offs.ptr);
     return MESH_OK;
 }
 

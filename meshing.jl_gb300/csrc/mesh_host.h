@@ -133,6 +133,7 @@ void set_types(Plan &P, int T, const mesh_params *p, int *Q64, int *A64, int *P6
 // each volume's table block offset in doubles, and the totals.
 struct BatchSizes {
     int64_t items = 0, pieces = 0, nflags = 0, tdoubles = 0, stiles = 0, max_ntab = 1;
+    int64_t keys = 0;  // lattice-edge keys of all volumes (3 per node)
 };
 BatchSizes tile_batch(const int64_t *dims, int n, int zs, std::vector<BatchVol> &hv, std::vector<int64_t> &tab_off);
 // The volume of every work item and scan tile.

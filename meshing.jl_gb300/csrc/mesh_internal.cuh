@@ -143,6 +143,7 @@ struct BatchVol {
     void *verts;
     int64_t *faces;
     int64_t vcap, fcap;
+    int64_t kbase;  // welded batches: the volume's lattice-edge keys start here
 };
 
 // Bytes per sample of a volume dtype.
@@ -213,6 +214,14 @@ int64_t weld_hash_slots(int64_t nv);
 cudaError_t launch_weld(const long long *vkey, int64_t nv, const void *verts, int out64, int64_t *faces, int64_t nf,
                         long long *bsum, void *wverts, unsigned long long *hkey, long long *hval, int64_t hcap,
                         unsigned *err, int sms, cudaStream_t s);
+// The same over a batch: the counts are read on the device (tot[0] vertices,
+// tot[1] faces, at most nvmax / nfmax), faces are 1-based within their volume
+// (first vertex / face of volume v at vol_off[2v], vol_off[2v + 1]; row n the
+// totals) before and after, and woff receives the welded rows.
+cudaError_t launch_weld_batch(const long long *vkey, int64_t nvmax, int64_t nfmax, const int64_t *tot,
+                              const void *verts, int out64, int64_t *faces, const int64_t *vol_off, int n,
+                              int64_t *woff, long long *bsum, void *wverts, unsigned long long *hkey, long long *hval,
+                              int64_t hcap, unsigned *err, int sms, cudaStream_t s);
 
 // Launchers (each returns cudaError_t of the launch).
 // xoff / nxt: the volume is x nodes xoff .. xoff+nx-1 of an axis of nxt nodes (0, 0: the whole axis).

@@ -420,15 +420,23 @@ __global__ void __launch_bounds__(XW) k_expand_mc(const Plan p) {
             vertex_task<T, Q, P>(p, MODE == EXP_BATCH ? batch_tabs(p, sm.vol[j]) : tb, ed, (int)(pos & pmask),
                                  (int)((pos >> POS_BITS) & pmask), (int)(pos >> (2 * POS_BITS)), sm.val[g & 7][j],
                                  sm.val[(g >> 3) & 7][j], vout, out);
-            if (MODE == EXP_ORDERED && p.vkey) {
+            if ((MODE == EXP_ORDERED || (MODE == EXP_BATCH && !p.vol_outputs)) && p.vkey) {
                 // the edge's lower node; the cell owns the edge when, across each
                 // other axis, the edge lies on the cell's upper side or the cell is first
+                // (in a batch, each volume's keys start at its own base)
                 const int x = (int)(pos & pmask), y = (int)((pos >> POS_BITS) & pmask), z = (int)(pos >> (2 * POS_BITS));
                 const int a = g & 7, ax = (g >> 6) & 3;
                 const int ox = ax == 0 ? 0 : cdx(a), oy = ax == 1 ? 0 : cdy(a), oz = ax == 2 ? 0 : cdz(a);
                 const bool own = (ax == 0 || ox || x == 0) && (ax == 1 || oy || y == 0) && (ax == 2 || oz || z == 0);
+                int64_t kx = p.nx, ky = p.ny, kb = 0;
+                if (MODE == EXP_BATCH) {
+                    const BatchVol &b = p.bvols[sm.vol[j]];
+                    kx = b.nx;
+                    ky = b.ny;
+                    kb = b.kbase;
+                }
                 const long long key =
-                    ax + 3 * ((long long)(x + ox) + p.nx * ((long long)(y + oy) + p.ny * (long long)(z + oz)));
+                    kb + ax + 3 * ((long long)(x + ox) + kx * ((long long)(y + oy) + ky * (long long)(z + oz)));
                 p.vkey[out] = key | (own ? (long long)(1ull << 63) : 0ll);
             }
         }

@@ -141,3 +141,53 @@ def test_uneven_batch_of_512(pkg, cuda):
     b.sync()
     check_alone(torch, pkg, b, vols, m, every=7)
     b.close()
+
+
+@pytest.mark.parametrize('dt', ['f32', 'f64', 'u16'])
+def test_welded_batch_matches_each_volume_alone(pkg, oracle, cuda, dt):
+    # MarchingCubes(weld=True) over a batch: each volume's welded mesh (its own
+    # rows of the welded offsets, faces 1-based within it) equals the welded
+    # isosurface() of the volume alone -- one run after the count, graph replays,
+    # and a run on changed contents with fewer crossings
+    torch = cuda
+    rng = np.random.default_rng(9)
+    ranges = None
+    if dt == 'u16':
+        shapes = [tuple(int(s) for s in rng.integers(3, 36, 3)) for _ in range(30)]
+        vols = [(torch.rand(sh, device='cuda') * 1000).to(torch.int32).to(torch.uint16) for sh in shapes]
+        m = pkg.MarchingCubes(iso=500, weld=True)
+        ranges = [((float(a), float(a) + 2.0), (-1.0, float(c)), (0.5, 3.0)) for a, c in rng.uniform(-2, 2, (30, 2))]
+    else:
+        vols = ragged(torch, 40, 7, 2, 44, torch.float32 if dt == 'f32' else torch.float64)
+        vols[3] = torch.zeros((1, 9, 9), device='cuda', dtype=vols[0].dtype)  # no cells
+        vols[11] = torch.ones((6, 5, 7), device='cuda', dtype=vols[0].dtype)   # cells, no crossings
+        m = pkg.MarchingCubes(iso=np.float32(0) if dt == 'f32' else 0.0, weld=True)
+    b = pkg.Batch(vols, m, ranges=ranges)
+    nv, nf = b.count()
+    check_alone(torch, pkg, b, vols, m, ranges)  # the count's own run
+    b.set_graph(True)
+    for _ in range(2):
+        b.run()
+        b.sync()
+    check_alone(torch, pkg, b, vols, m, ranges)
+    if dt != 'u16':
+        for i in (0, 5, 39):
+            A = np.asfortranarray(vols[i].cpu().numpy())
+            want = oracle.isosurface(A, 'mcw', m.iso, 1e-3, ((-1, 1),) * 3)
+            v, f = b.volume(i)
+            assert_same((v.cpu().numpy(), f.cpu().numpy()), want, 'welded batch volume %d' % i)
+        # the per-cell batch of the same volumes: same faces, more vertices
+        c = pkg.Batch(vols, pkg.MarchingCubes(iso=m.iso))
+        nv_cell, nf_cell = c.count()
+        assert nf_cell == nf and nv < nv_cell
+        c.close()
+        # fewer crossings after the count: a run reports the new welded rows
+        vols[5].copy_(torch.full_like(vols[5], 1.0))
+        b.run()
+        b.sync()
+        offs = b.outputs()[2].cpu().numpy()
+        v5 = offs[6] - offs[5]
+        assert v5.tolist() == [0, 0]
+        b.nverts, b.nfaces = (int(x) for x in offs[-1])
+        check_alone(torch, pkg, b, vols, m, ranges)
+    b.close()
