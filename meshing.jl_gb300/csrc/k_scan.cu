@@ -15,6 +15,9 @@
 // and the warps walk their runs again writing the offsets.  No wait between
 // CTAs.
 //
+// Batch of small volumes (k_scan_batch_vol): one CTA per volume, chained over
+// the volumes (below).
+//
 // Batch (k_scan_batch): one CTA scans 32 columns of one volume: its warps
 // split the (y, seg) sequence of every column, reduce, scan across warps
 // through shared memory (one warp per counter: vertices, faces, active cells),
@@ -401,6 +404,130 @@ __global__ void __launch_bounds__(1024) k_scan_batch(const Plan p) {
     scan_body(vol_view(p, b), t - b.stile0, t, p.nstiles, s_part, s_xpre);
 }
 
+// Batch of small volumes (every volume at most a few 32-column groups wide),
+// one CTA per volume in ticket order: the volume's groups are reduced to its
+// totals, one decoupled look-back over the volumes gives its offset, and the
+// groups are scanned again in x order from that offset (the second read of the
+// counts mostly hits the caches).  A chain of volumes instead of groups, and a
+// CTA's fixed costs paid once per volume.
+__global__ void __launch_bounds__(1024) k_scan_batch_vol(const Plan p) {
+    __shared__ int s_v;
+    __shared__ int64_t s_part[NCNT][32][33];
+    __shared__ int64_t s_xpre[NCNT][32];
+    __shared__ int64_t s_run[NCNT];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) s_v = (int)atomicAdd(p.scan_ticket, 1u);
+    if (threadIdx.x < NCNT) s_run[threadIdx.x] = 0;
+    __syncthreads();
+    const int v = s_v;
+    const BatchVol bv = p.bvols[v];
+    const Plan q = vol_view(p, bv);
+    const int T = bv.cx ? (bv.cx + 31) / 32 : 0;
+    const int64_t L = (int64_t)q.cy * q.nseg;
+    const int64_t per = (L + nw - 1) / nw;
+    const int64_t j0 = min(L, (int64_t)w * per), j1 = min(L, j0 + per);
+    const int64_t np = q.pstride;
+    const int64_t dseg = (int64_t)q.cy * q.cx, wrap = (int64_t)q.cx - (int64_t)(q.nseg - 1) * dseg;
+    // the lane's column sums over the warp's (y, seg) range in tile xt
+    auto partial = [&](int xt, int64_t (&sum)[NCNT]) {
+        const int x = xt * 32 + lane;
+#pragma unroll
+        for (int c = 0; c < NCNT; c++) sum[c] = 0;
+        if (x >= q.cx) return;
+        int seg = (int)(j0 % q.nseg);
+        int64_t i = piece(q, seg, (int)(j0 / q.nseg), x);
+        for (int64_t j = j0; j < j1; j++) {
+#pragma unroll
+            for (int c = 0; c < NCNT; c++) sum[c] += q.cnt[c * np + i];
+            if (++seg == q.nseg) {
+                seg = 0;
+                i += wrap;
+            } else {
+                i += dseg;
+            }
+        }
+    };
+    // pass 1: the volume's totals
+    int64_t acc[NCNT] = {0, 0, 0};
+    for (int xt = 0; xt < T; xt++) {
+        int64_t sum[NCNT];
+        partial(xt, sum);
+#pragma unroll
+        for (int c = 0; c < NCNT; c++) acc[c] += sum[c];
+    }
+    // block reduce per counter
+#pragma unroll
+    for (int c = 0; c < NCNT; c++) {
+        int64_t a = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(FULL, a, o);
+        if (lane == 0) s_part[c][w][0] = a;
+    }
+    __syncthreads();
+    if (w < NCNT) {
+        const int c = w;
+        int64_t a = lane < nw ? s_part[c][lane][0] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(FULL, a, o);
+        if (lane == 0) {
+            const int64_t pre = look_back(p.scan_state + (int64_t)c * p.nvols, v, a, p.scan_spin_limit, p.err);
+            s_run[c] = pre;
+            if (v == p.nvols - 1) p.totals[c] = pre + a;
+        }
+    }
+    __syncthreads();
+    // pass 2: every tile from the running offset
+    for (int xt = 0; xt < T; xt++) {
+        int64_t sum[NCNT];
+        partial(xt, sum);
+#pragma unroll
+        for (int c = 0; c < NCNT; c++) s_part[c][w][lane] = sum[c];
+        __syncthreads();
+        if (w < NCNT) {
+            const int c = w;
+            int64_t tot = 0;
+            for (int k = 0; k < nw; k++) {
+                const int64_t a = s_part[c][k][lane];
+                s_part[c][k][lane] = tot;
+                tot += a;
+            }
+            int64_t inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t a = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc += a;
+            }
+            s_xpre[c][lane] = s_run[c] + inc - tot;
+            __syncwarp();
+            if (lane == 31) s_run[c] += inc;
+        }
+        __syncthreads();
+        const int x = xt * 32 + lane;
+        if (x < q.cx) {
+            int64_t b[NCNT];
+#pragma unroll
+            for (int c = 0; c < NCNT; c++) b[c] = s_xpre[c][lane] + s_part[c][w][lane];
+            int seg = (int)(j0 % q.nseg);
+            int64_t i = piece(q, seg, (int)(j0 / q.nseg), x);
+            for (int64_t j = j0; j < j1; j++) {
+#pragma unroll
+                for (int c = 0; c < NCNT; c++) {
+                    const uint32_t cv = q.cnt[c * np + i];
+                    q.base[c * np + i] = b[c];
+                    b[c] += cv;
+                }
+                if (++seg == q.nseg) {
+                    seg = 0;
+                    i += wrap;
+                } else {
+                    i += dseg;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // First vertex / face of every volume: the scanned offset of its first piece
 // in emission order (x = y = seg = 0).  A volume without cells shares the
 // offset of the next piece, or the totals.
@@ -427,7 +554,16 @@ size_t scan_scratch_bytes(const Plan &p) {
     return (size_t)NCNT * 32 * g.G * (g.C + 1) * sizeof(long long);  // run sums, column sums
 }
 
-cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s) {
+cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s, bool per_volume) {
+    if (per_volume && p.nvols > 0) {
+        cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * NCNT * (size_t)p.nvols, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p.scan_ticket, 0, sizeof(unsigned int), s);
+        if (e != cudaSuccess) return e;
+        k_scan_batch_vol<<<p.nvols, threads, 0, s>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        k_batch_offsets<<<(p.nvols + 1 + 255) / 256, 256, 0, s>>>(p);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaMemsetAsync(p.scan_state, 0, sizeof(unsigned long long) * NCNT * (size_t)p.nstiles, s);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(p.scan_ticket, 0, sizeof(unsigned int), s);

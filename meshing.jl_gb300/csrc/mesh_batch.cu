@@ -41,6 +41,7 @@ struct mesh_batch {
     int zs = 0;                   // z cells per work item, a multiple of ZC; 0 = whole columns
     int cls_ctas = 0, cmp_ctas = 0;  // CTAs per SM of the persistent kernels; 0 = as many as fit
     int scan_threads = 1024;
+    bool scan_vol = false;        // every volume at most 4 column groups wide: the per-volume scan
     Plan P{};
     std::vector<BatchVol> hv;
     DevBuf dvols, ivol, svol, tabs, jobs, cnt, base, flags, scan, misc, ent, out_v, out_f, offs;
@@ -146,7 +147,7 @@ int build_plan(mesh_batch *b) {
         (e = b->cnt.ensure((size_t)pieces * NCNT * 4 + 4)) != cudaSuccess ||
         (e = b->base.ensure((size_t)pieces * NCNT * 8 + 8)) != cudaSuccess ||
         (e = b->flags.ensure((size_t)nflags + 1)) != cudaSuccess ||
-        (e = b->scan.ensure((size_t)stiles * NCNT * 8 + 64)) != cudaSuccess ||
+        (e = b->scan.ensure((size_t)std::max<int64_t>(stiles, n) * NCNT * 8 + 64)) != cudaSuccess ||
         (e = b->misc.ensure(MISC_SLOTS * sizeof(int64_t))) != cudaSuccess ||
         (e = b->offs.ensure((size_t)(n + 1) * 2 * 8)) != cudaSuccess)
         return cuda_fail(c, e, "batch buffers");
@@ -182,7 +183,9 @@ int build_plan(mesh_batch *b) {
     P.base = (int64_t *)b->base.ptr;
     P.flags = (uint8_t *)b->flags.ptr;
     P.scan_state = (unsigned long long *)b->scan.ptr;
-    P.scan_ticket = (unsigned int *)((char *)b->scan.ptr + (size_t)stiles * NCNT * 8);
+    P.scan_ticket = (unsigned int *)((char *)b->scan.ptr + (size_t)std::max<int64_t>(stiles, n) * NCNT * 8);
+    b->scan_vol = true;
+    for (const BatchVol &bv : b->hv) b->scan_vol = b->scan_vol && bv.cx <= 4 * 32;
     P.totals = (int64_t *)b->misc.ptr;
     P.err = (unsigned int *)((int64_t *)b->misc.ptr + NCNT);
     P.work = (unsigned int *)((int64_t *)b->misc.ptr + NCNT + 1);
@@ -217,7 +220,8 @@ int enqueue_count(mesh_batch *b, cudaStream_t s) {
     if ((e = cudaMemsetAsync(b->misc.ptr, 0, MISC_SLOTS * sizeof(int64_t), s)) != cudaSuccess)
         return cuda_fail(c, e, "memset");
     if ((e = launch_classify_batch(b->P, b->cls_ctas, s)) != cudaSuccess) return cuda_fail(c, e, "batch classify");
-    if ((e = launch_scan_batch(b->P, b->scan_threads, s)) != cudaSuccess) return cuda_fail(c, e, "batch scan");
+    if ((e = launch_scan_batch(b->P, b->scan_threads, s, b->scan_vol)) != cudaSuccess)
+        return cuda_fail(c, e, "batch scan");
     return MESH_OK;
 }
 

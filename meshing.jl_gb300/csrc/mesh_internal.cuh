@@ -238,7 +238,9 @@ cudaError_t launch_tables_batch(const TabJob *jobs, int njobs, int64_t max_ntab,
 // ctas: CTAs per SM of the persistent kernels (0 = as many as fit), threads:
 // threads per scan CTA.
 cudaError_t launch_classify_batch(const Plan &p, int ctas, cudaStream_t s);
-cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s);
+// per_volume: every volume is at most a few 32-column groups wide -- chain the
+// volumes, one CTA each (scan state for NCNT x nvols entries)
+cudaError_t launch_scan_batch(const Plan &p, int threads, cudaStream_t s, bool per_volume = false);
 cudaError_t launch_compact_batch(const Plan &p, int ctas, cudaStream_t s);
 cudaError_t launch_expand_batch(const Plan &p, int Q64, int P64, cudaStream_t s);
 cudaError_t launch_classify(const Plan &p, cudaStream_t s, int seg0 = 0, int nsegs = 0);  // nsegs 0: all
