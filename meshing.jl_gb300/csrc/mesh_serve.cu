@@ -211,6 +211,7 @@ struct GroupLayout {
     size_t o_tabs = 0, o_cnt = 0, o_base = 0, o_flags = 0, o_scan = 0, o_misc = 0, o_offs = 0;
     size_t o_pos = 0, o_val = 0, o_side = 0, o_vol = 0, o_cs = 0, total = 0;
     int64_t cells = 0;
+    bool scan_vol = false;  // the per-volume scan (every volume at most 128 columns wide)
 };
 
 
@@ -224,6 +225,9 @@ void layout_group(const std::vector<const Req *> &rs, GroupLayout *L) {
             L->cells += (dims[3 * i] - 1) * (dims[3 * i + 1] - 1) * (dims[3 * i + 2] - 1);
     }
     L->z = tile_batch(dims.data(), n, 0, L->hv, L->tab_off);
+    // every volume at most 4 column groups wide: one scan CTA per volume, chained
+    L->scan_vol = n > 0;
+    for (const BatchVol &bv : L->hv) L->scan_vol = L->scan_vol && bv.cx <= 4 * 32;
     const BatchSizes &z = L->z;
     const size_t es = n ? dtype_size(rs[0]->T) : 4;
     size_t o = up(sizeof(BatchVol) * (size_t)std::max(n, 1));
@@ -235,7 +239,7 @@ void layout_group(const std::vector<const Req *> &rs, GroupLayout *L) {
     L->o_cnt = o; o += up((size_t)z.pieces * NCNT * 4 + 4);
     L->o_base = o; o += up((size_t)z.pieces * NCNT * 8 + 8);
     L->o_flags = o; o += up((size_t)z.nflags + 1);
-    L->o_scan = o; o += up((size_t)z.stiles * NCNT * 8 + 64);
+    L->o_scan = o; o += up((size_t)std::max<int64_t>(z.stiles, n) * NCNT * 8 + 64);
     L->o_misc = o; o += up(MISC_SLOTS * 8);
     L->o_offs = o; o += up((size_t)(n + 1) * 16);
     const size_t cap = (size_t)L->cells;  // worst case: every cell active
@@ -251,7 +255,7 @@ void layout_group(const std::vector<const Req *> &rs, GroupLayout *L) {
 // layout_group grows by at most this much when r joins (before rounding).
 size_t vol_scratch_bytes(const Req &r) {
     const int64_t nx = r.dims[0], ny = r.dims[1], nz = r.dims[2];
-    size_t b = sizeof(BatchVol) + sizeof(TabJob) + 16 + 4 + 4 + 8;
+    size_t b = sizeof(BatchVol) + sizeof(TabJob) + 16 + 4 + 4 + 8 + NCNT * 8;
     if (nx > 1 && ny > 1 && nz > 1) {
         const int64_t cx = nx - 1, cy = ny - 1, cz = nz - 1, cells = cx * cy * cz;
         const int64_t zs = (cz + ZC - 1) / ZC * ZC;
@@ -691,7 +695,7 @@ int launch_wave(mesh_server *s, Slot &sl) {
         P.base = (int64_t *)(blk + L.o_base);
         P.flags = (uint8_t *)(blk + L.o_flags);
         P.scan_state = (unsigned long long *)(blk + L.o_scan);
-        P.scan_ticket = (unsigned int *)(blk + L.o_scan + (size_t)L.z.stiles * NCNT * 8);
+        P.scan_ticket = (unsigned int *)(blk + L.o_scan + (size_t)std::max<int64_t>(L.z.stiles, n) * NCNT * 8);
         P.totals = (int64_t *)(blk + L.o_misc);
         P.err = (unsigned int *)((int64_t *)(blk + L.o_misc) + NCNT);
         P.work = (unsigned int *)((int64_t *)(blk + L.o_misc) + NCNT + 1);
@@ -713,7 +717,7 @@ int launch_wave(mesh_server *s, Slot &sl) {
         P.verts_cap = P.faces_cap = (int64_t)1 << 62;  // each volume checks its own block
         if ((e = cudaMemsetAsync(blk + L.o_misc, 0, MISC_SLOTS * 8, sl.stream)) != cudaSuccess ||
             (e = launch_classify_batch(P, 0, sl.stream)) != cudaSuccess ||
-            (e = launch_scan_batch(P, 256, sl.stream)) != cudaSuccess ||
+            (e = launch_scan_batch(P, L.scan_vol ? 1024 : 256, sl.stream, L.scan_vol)) != cudaSuccess ||
             (e = launch_compact_batch(P, 0, sl.stream)) != cudaSuccess ||
             (e = launch_expand_batch(P, Q64, P64, sl.stream)) != cudaSuccess ||
             (e = cudaMemcpyAsync(sl.res + g.res_off, P.vol_off, 16 * (size_t)(n + 1), cudaMemcpyDeviceToHost,
