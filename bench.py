@@ -610,7 +610,7 @@ def measure_serving(args, rank, world, dev):
         iso = np.float32(0) if dt == torch.float32 else 0.0
         return [pkg.MarchingCubes, pkg.MarchingTetrahedra, pkg.NaiveSurfaceNets][a](iso=iso)
 
-    srv = pkg.Server(budget_bytes=int(args.budget_gb * 1e9), slots=3, max_wave=256, max_queue=args.max_queue,
+    srv = pkg.Server(budget_bytes=int(args.budget_gb * 1e9), slots=args.slots, max_wave=256, max_queue=args.max_queue,
                      device=local)
     # warm-up (pinned staging, context scratch, kernel caches), not measured
     warm = [(A, method(a, A.dtype), r) for A, r in pool for a in range(3)]
@@ -697,7 +697,7 @@ def measure_serving(args, rank, world, dev):
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32/f64', 'data': 'synthetic',
         'config': {'workload': 'Poisson arrivals; cubic sizes log-uniform 32..512; 50/50 Float32 / Float64; random '
                                'sines on [0,1]^3 or primitive SDFs on [-1,1]^3; 60/30/10 MC / MT / NSN; iso 0',
-                   'budget_gb': args.budget_gb, 'slots': 3, 'max_wave': 256, 'max_queue': args.max_queue,
+                   'budget_gb': args.budget_gb, 'slots': args.slots, 'max_wave': 256, 'max_queue': args.max_queue,
                    'volume_pool': args.pool},
         'sweep': sweep,
         'saturation_per_s': max(x['throughput_per_s'] for x in sweep),
@@ -880,6 +880,7 @@ def main():
     ap.add_argument('--volumes', type=int, default=4096, help='volumes of the batched workload')
     ap.add_argument('--pool', type=int, default=40, help='serving: distinct resident request volumes')
     ap.add_argument('--budget-gb', type=float, default=120.0, help='serving: device memory budget')
+    ap.add_argument('--slots', type=int, default=6, help='serving: waves in flight at once')
     ap.add_argument('--rate0', type=float, default=400.0,
                     help='serving: first offered rate (requests per second); doubled until the loop saturates')
     ap.add_argument('--max-rates', type=int, default=8, help='serving: at most this many offered rates')
