@@ -79,6 +79,31 @@ struct NsnPairs {
 
 __device__ __forceinline__ uint32_t lanemask_le(int lane) { return (2u << lane) - 1u; }
 
+// a / n for a vertex's crossing count n (1..12), rounded exactly as the IEEE
+// division, from one product and two fused operations (division by a small
+// constant after Markstein, IBM J. Res. Develop. 34(1), 1990).  With y = RN(1/n)
+// (rcp[n]) and q = RN(a*y), within 1.5 ulps of a/n and |q| <= |a|, the
+// remainder a - q*n is a multiple of ulp(q) below 18 ulps: the fma computes it
+// exactly.  q + r*y = a/n + r*(y - 1/n) then lies within 36 * 2^-53 ulps of
+// a/n, while a/n is at least ulp/24 away from every rounding midpoint: n is
+// 2^j times an odd number o, a/2^j is exact, and a - n*M for a midpoint M is a
+// nonzero multiple of ulp/2.  So the one rounding of q + r*y gives RN(a/n).
+// Zeros, |a| below 2^-959 (where a/2^j could round) and Inf / NaN take the
+// division.
+__device__ __forceinline__ double div_count(double a, int n, const double *rcp) {
+    const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ffu;
+    if (e < 64u || e == 0x7ffu) return __ddiv_rn(a, (double)n);
+    const double y = rcp[n], q = __dmul_rn(a, y);
+    return __fma_rn(__fma_rn(-q, (double)n, a), y, q);
+}
+// The same in Float32 (24-bit significands; |a| below 2^-63 takes the division).
+__device__ __forceinline__ float div_count(float a, int n, const float *rcp) {
+    const unsigned e = (__float_as_uint(a) >> 23) & 0xffu;
+    if (e < 64u || e == 0xffu) return __fdiv_rn(a, (float)n);
+    const float y = rcp[n], q = __fmul_rn(a, y);
+    return __fmaf_rn(__fmaf_rn(-q, (float)n, a), y, q);
+}
+
 // First entry of the inclusive prefix a[0..n) above t (a[n-1] > t).
 __device__ __forceinline__ int task_cell(const uint16_t *a, int n, int t) {
     int lo = 0, hi = n - 1;
@@ -145,7 +170,9 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
     MtTables *tb = reinterpret_cast<MtTables *>(smem + sizeof(HaloWarp<T>) * WARPS);  // MT
     NsnPairs *prs = reinterpret_cast<NsnPairs *>(smem + sizeof(HaloWarp<T>) * WARPS);  // NSN
     __shared__ uint16_t s_cross[256];  // NSN: the crossed MC edges of each MC case
+    __shared__ P s_rcp[13];            // NSN: RN(1/n) for the crossing counts n
     if (ALG == MESH_ALG_NSN) {
+        if (threadIdx.x <= 12) s_rcp[threadIdx.x] = threadIdx.x ? Ar<P>::div(P(1), (P)threadIdx.x) : P(0);
         for (int c = threadIdx.x; c < 256; c += blockDim.x) {
             // edges 0-7 join corners e, e+1 of their face ring, 8-11 join e-8 and e-4
             unsigned m = 0;
@@ -292,9 +319,9 @@ __global__ void __launch_bounds__(256, 3) k_emit_halo(const Plan p, int tiles_xh
         if (ALG != MESH_ALG_NSN) return;
         NsnPairs &pr = prs[wid];
         if (lane < m) {
-            const P n = (P)pr.qn[lane];
-            store_vert(p, pr.qv[lane], Ar<P>::div((P)pr.qs[lane][0], n), Ar<P>::div((P)pr.qs[lane][1], n),
-                       Ar<P>::div((P)pr.qs[lane][2], n));
+            const int n = pr.qn[lane];
+            store_vert(p, pr.qv[lane], div_count((P)pr.qs[lane][0], n, s_rcp), div_count((P)pr.qs[lane][1], n, s_rcp),
+                       div_count((P)pr.qs[lane][2], n, s_rcp));
         }
         __syncwarp();
     };
