@@ -887,7 +887,7 @@ def main():
     ap.add_argument('--max-queue', type=int, default=1024, help='serving: waiting requests beyond which the loop '
                                                                 'rejects (MESH_EBUSY)')
     ap.add_argument('--requests', type=int, default=1500, help='serving: requests per rate (at most)')
-    ap.add_argument('--rates128', default='60000,120000,160000,200000',
+    ap.add_argument('--rates128', default='60000,120000,160000,200000,240000',
                     help='serving 128^3: offered requests per second')
     ap.add_argument('--requests128', type=int, default=60000, help='serving 128^3: requests per rate (at most)')
     args = ap.parse_args()
