@@ -21,7 +21,7 @@ one of them alone):
   batched -- 4096 uneven Float32 volumes in one tuned, graph-replayed batch,
              against a loop of per-volume calls;
   serving -- Poisson arrivals of mixed requests (32^3..512^3, Float32/Float64,
-             60/30/10 MC/MT/NSN) under a 120 GB budget, the offered rate
+             60/30/10 MC/MT/NSN) under a 120 GB budget on 6 slots, the offered rate
              doubled until the loop saturates; 128^3 MC requests against a
              batch of the same 256 distinct volumes;
   gyroid  -- MC, MT and NSN on the Float32 256^3 gyroid;
