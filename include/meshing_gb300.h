@@ -254,7 +254,10 @@ MESH_API int mesh_batch_tune(mesh_batch *b, int reps, char *report, int report_l
  * Tetrahedra, 1 vertex per cell and 6 faces per node for Naive Surface Nets.
  * Marching Cubes requests of a wave with the same volume type and iso run as
  * one batch; waves on different slots overlap on the device.  A request's mesh
- * stays resident in the pool until mesh_server_release.  Thread-safe. */
+ * stays resident in the pool until mesh_server_release.  Thread-safe.
+ * slots (1..16): waves in flight at once, each capped at budget_bytes / slots
+ * beyond its first request; max_wave: requests per wave; max_queue: waiting
+ * requests beyond which mesh_server_submit rejects (MESH_EBUSY). */
 typedef struct mesh_server mesh_server;
 MESH_API int mesh_server_create(int device, int64_t budget_bytes, int slots, int max_wave, int max_queue,
                                 mesh_server **out);
